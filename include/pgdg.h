@@ -1,0 +1,99 @@
+/*
+ * pgdg.h -- C ABI of libpgdg_gpu.so, the GB300-native per-time-step
+ * particle-grid path of the Particle-Grid DG method (reference: PGDG_p2,
+ * program 3D_generalized/PGDG_3D_spheric; file:line citations below are
+ * relative to that program unless another program is named).
+ *
+ * The reference has no plugin or FFI: its boundary is the MPM method set that
+ * the driver calls (mpm.h:160-194) with all state inside the MPM object.  Each
+ * entry point below replaces one of those methods; the state lives in an opaque
+ * context on one GPU.  Every function returns PGDG_OK (0) or a negative
+ * PGDG_E* code; pgdg_last_error() describes the last failure.  Calls on one
+ * context are stream-ordered and not re-entrant; separate contexts are
+ * independent.
+ */
+#ifndef PGDG_H
+#define PGDG_H
+#include "pgdg_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pgdg_ctx pgdg_ctx;
+
+/* precision of the grid/particle arithmetic */
+enum { PGDG_PREC_FP64 = 0, PGDG_PREC_MIXED = 1 };
+/* MGFM Newton seed */
+enum { PGDG_SEED_PLAIN = 0, PGDG_SEED_MLP = 1 };
+
+/* ---- case construction (replaces MPM::Initialize_case, mpm_ini.cpp:33-673) ----
+ * config_id 1..4 are the synthetic workloads: 1 2D triple point 112x48,
+ * 2 3D cylinder shock-bubble 256x64x64, 3 3D sphere shock-bubble 384x96x96,
+ * 4 2D underwater explosion 1024^2.  ncell (may be NULL) overrides the grid. */
+int pgdg_case_setup(int config_id, const int32_t* ncell, pgdg_case* out);
+int64_t pgdg_case_num_particles(const pgdg_case* cs);
+int pgdg_case_particles(const pgdg_case* cs, int config_id, uint64_t seed, pgdg_particles* out);
+int pgdg_case_cells(const pgdg_case* cs, pgdg_cells* out);
+
+/* ---- context ---- */
+/* MPM::MPM + allocation; capacity = max fluid particles held (0 = automatic) */
+int pgdg_create(const pgdg_case* cs, int precision, int64_t capacity, pgdg_ctx** out);
+int pgdg_destroy(pgdg_ctx* ctx);
+const char* pgdg_last_error(pgdg_ctx* ctx);
+int pgdg_capacity(pgdg_ctx* ctx, int64_t* cap);
+
+/* ---- data movement (host arrays, canonical particle order) ---- */
+int pgdg_upload_particles(pgdg_ctx* ctx, const pgdg_particles* p);
+int pgdg_download_particles(pgdg_ctx* ctx, pgdg_particles* p); /* p->n: in capacity, out count */
+int pgdg_num_particles(pgdg_ctx* ctx, int64_t* n);
+int pgdg_upload_cells(pgdg_ctx* ctx, const pgdg_cells* c);
+int pgdg_download_cells(pgdg_ctx* ctx, pgdg_cells* c);
+/* Particle_base::neighbor lists, canonical index space (>=0 fluid index,
+ * -1 dead particle, -(2+b) boundary particle b); stored[i] says whether the
+ * device holds particle i's list (it keeps only the lists split/merge read). */
+int pgdg_upload_lists(pgdg_ctx* ctx, const int64_t* off, const int64_t* ent);
+int pgdg_download_lists(pgdg_ctx* ctx, int64_t* off, int64_t* ent, int32_t* stored, int64_t cap,
+                        int64_t* total);
+/* Cell_list::particle_list of every cell (cell_list.h), same encoding */
+int pgdg_download_cell_lists(pgdg_ctx* ctx, int64_t* off, int64_t* ent, int64_t cap, int64_t* total);
+
+int pgdg_set_dt(pgdg_ctx* ctx, double dt);                 /* Solver clip of glbl_timestep (solver.cpp:40-44) */
+int pgdg_set_iterate(pgdg_ctx* ctx, int64_t iterate_num);
+int pgdg_set_max_v(pgdg_ctx* ctx, double max_v);
+int pgdg_set_seed_mode(pgdg_ctx* ctx, int mode);           /* PGDG_SEED_PLAIN / PGDG_SEED_MLP */
+int pgdg_get_stats(pgdg_ctx* ctx, pgdg_stats* st);
+int pgdg_synchronize(pgdg_ctx* ctx);
+
+/* ---- reference methods ---- */
+int pgdg_set_timestep(pgdg_ctx* ctx, double* dt, double* max_v);   /* MPM::Set_timestep mpm.cpp:19-57 */
+int pgdg_used_state_update(pgdg_ctx* ctx);                         /* mpm.cpp:184-263 */
+int pgdg_bin_particles(pgdg_ctx* ctx);                             /* Reset_cell_list_info + Map_the_particle_to_tree mpm.cpp:65-96 */
+int pgdg_split_particle_fast(pgdg_ctx* ctx);                       /* mpm.cpp:1036-1417 */
+int pgdg_merge_particle_fast(pgdg_ctx* ctx);                       /* mpm.cpp:1536-1706 (one pass) */
+int pgdg_refresh_membership(pgdg_ctx* ctx);                        /* Reset/Refresh_neighbor_info(4) mpm.cpp:101-161 */
+int pgdg_refresh_neighbors(pgdg_ctx* ctx);                         /* Reset/Refresh_neighbor_info(2) level_infor.cpp:153-195 */
+int pgdg_mls_p2g(pgdg_ctx* ctx);                                   /* MPM::MLS_P2G mpm.cpp:274-382 */
+int pgdg_calculate_limiter(pgdg_ctx* ctx);                         /* mpm.cpp:392-738 */
+int pgdg_grid_acceleration(pgdg_ctx* ctx);                         /* mpm.cpp:747-763 -> particle_flow.cpp:16-405 */
+int pgdg_update_grid(pgdg_ctx* ctx, int md);                       /* mpm.cpp:768-830 */
+int pgdg_update_particle(pgdg_ctx* ctx, int md);                   /* mpm.cpp:839-853 -> particle_flow.cpp:413-622 */
+int pgdg_run_step(pgdg_ctx* ctx, int64_t n);                       /* MPM::MPM_run_simulation mpm_ini.cpp:682-766 */
+/* Solver::MPM_Solver (solver.cpp:30-64) without output clipping:
+ * nsteps x {Set_timestep, ++iterate_num, MPM_run_simulation}, all on device */
+int pgdg_advance(pgdg_ctx* ctx, int nsteps);
+int pgdg_totals(pgdg_ctx* ctx, double* out6);                      /* conservation totals (Triple_point_2phase/mpm_ini.cpp:599-654) */
+
+/* ---- MGFM interface Riemann solve (mpm.cpp:882-926), batched ----
+ * in6: n x (u_l, u_r, p_l, p_r, rho_l, rho_r); mat2: n x (material l, material r)
+ * into gam/pinf (nmat entries); out3: n x (rho*_L, p*, u*); iters may be NULL.
+ * Pointers are device pointers; stream 0 ordering; seed_mode selects the plain
+ * max(p_l,p_r) start or the learned start. */
+int pgdg_mgfm_batched(pgdg_ctx* ctx, const double* in6, const int8_t* mat2, const double* gam,
+                      const double* pinf, int nmat, int variant, int seed_mode, double* out3,
+                      int32_t* iters, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -22,8 +22,13 @@ extern "C" {
 
 typedef struct pgdg_ctx pgdg_ctx;
 
-/* precision of the grid/particle arithmetic */
-enum { PGDG_PREC_FP64 = 0, PGDG_PREC_MIXED = 1 };
+/* precision of the grid/particle arithmetic:
+ *   FP64      all FP64, evaluated in the oracle's operation order without FMA
+ *             contraction (bit-identical to the CPU restatement of the reference)
+ *   MIXED     FP32 residual/limiter/G2P/shifting, FP64 MGFM Newton and P2G sums
+ *   FP64_FMA  all FP64 with FMA contraction (the plain FP64 GPU path timed
+ *             against MIXED) */
+enum { PGDG_PREC_FP64 = 0, PGDG_PREC_MIXED = 1, PGDG_PREC_FP64_FMA = 2 };
 /* MGFM Newton seed */
 enum { PGDG_SEED_PLAIN = 0, PGDG_SEED_MLP = 1 };
 

@@ -1,0 +1,88 @@
+"""Build of libpgdg_gpu.so for sm_103a (in tree, nvcc only, no cmake).
+
+Each CUDA translation unit is compiled in parallel to an object, then linked into
+pgdg_p2_gb300/_build/libpgdg_gpu.so.  k_particles.cu (split/merge/binning) is
+compiled with -fmad=false so its FP64 arithmetic matches the oracle bit for bit.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libpgdg_gpu.so")
+INC = os.path.join(os.path.dirname(HERE), "include")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# (source, object tag, extra flags): the grid and G2P kernels are compiled twice,
+# once with FMA contraction (mixed and FP64_FMA paths) and once without
+# (-DPGDG_EXACT_TU: the exact-order FP64 path)
+CU = [("k_particles.cu", "k_particles", ["-fmad=false"]),
+      ("k_grid.cu", "k_grid", []),
+      ("k_grid.cu", "k_grid_x", ["-fmad=false", "-DPGDG_EXACT_TU"]),
+      ("k_g2p.cu", "k_g2p", []),
+      ("k_g2p.cu", "k_g2p_x", ["-fmad=false", "-DPGDG_EXACT_TU"]),
+      ("k_mgfm.cu", "k_mgfm", ["-fmad=false"]),
+      ("capi.cu", "capi", [])]
+CPP = ["case_builder.cpp"]
+
+
+def _nvcc():
+    p = shutil.which("nvcc")
+    if p:
+        return p
+    for c in ("/usr/local/cuda/bin/nvcc",):
+        if os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _deps():
+    d = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    d += [os.path.join(INC, f) for f in os.listdir(INC)]
+    return d
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OUT, exist_ok=True)
+    if not force and os.path.exists(LIB):
+        t = os.path.getmtime(LIB)
+        if all(os.path.getmtime(x) <= t for x in _deps()):
+            return LIB
+    nvcc = _nvcc()
+    jobs = []
+    for f, tag, extra in CU:
+        obj = os.path.join(OUT, tag + ".o")
+        cmd = [nvcc] + ARCH + extra + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                                       "-I", INC, "-c", os.path.join(CSRC, f), "-o", obj]
+        jobs.append((cmd, obj))
+    for f in CPP:
+        obj = os.path.join(OUT, f + ".o")
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INC, "-c",
+               os.path.join(CSRC, f), "-o", obj]
+        jobs.append((cmd, obj))
+
+    def run(job):
+        cmd, obj = job
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(run, jobs))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

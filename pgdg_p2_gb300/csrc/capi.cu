@@ -1,0 +1,834 @@
+/*
+ * capi.cu -- the C ABI of libpgdg_gpu.so (include/pgdg.h) and the host driver.
+ *
+ * One context owns all device buffers of one case on one GPU and one CUDA
+ * stream.  The host driver restates the reference's call order:
+ * Solver::MPM_Solver (solver.cpp:30-64) -> MPM::Set_timestep -> MPM_run_simulation
+ * (mpm_ini.cpp:682-766).  No host synchronisation happens inside a step; dt,
+ * max_v and the particle counters live on the device.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pgdg.h"
+#include "pgdg_dev.cuh"
+
+using namespace pgdg;
+
+struct pgdg_ctx {
+  virtual ~pgdg_ctx() {}
+  std::string err;
+  pgdg_case cs;
+  int precision = PGDG_PREC_FP64;
+  int seed_mode = PGDG_SEED_PLAIN;
+  int64_t iterate = 0;
+  cudaStream_t st = nullptr;
+  virtual int upload_particles(const pgdg_particles*) = 0;
+  virtual int download_particles(pgdg_particles*) = 0;
+  virtual int num_particles(int64_t*) = 0;
+  virtual int upload_cells(const pgdg_cells*) = 0;
+  virtual int download_cells(pgdg_cells*) = 0;
+  virtual int upload_lists(const int64_t*, const int64_t*) = 0;
+  virtual int download_lists(int64_t*, int64_t*, int32_t*, int64_t, int64_t*) = 0;
+  virtual int download_cell_lists(int64_t*, int64_t*, int64_t, int64_t*) = 0;
+  virtual int set_dt(double) = 0;
+  virtual int set_max_v(double) = 0;
+  virtual int stats(pgdg_stats*) = 0;
+  virtual int capacity(int64_t*) = 0;
+  virtual int set_timestep(double*, double*) = 0;
+  virtual int used_state() = 0;
+  virtual int bin() = 0;
+  virtual int split() = 0;
+  virtual int merge() = 0;
+  virtual int refresh_membership() = 0;
+  virtual int refresh_neighbors() = 0;
+  virtual int p2g() = 0;
+  virtual int limiter() = 0;
+  virtual int grid_acc() = 0;
+  virtual int update_grid(int) = 0;
+  virtual int update_particle(int) = 0;
+  virtual int run_step(int64_t) = 0;
+  virtual int advance(int) = 0;
+  virtual int totals(double*) = 0;
+  virtual int check() = 0;
+};
+
+namespace {
+
+#define CK(x)                                                   \
+  do {                                                          \
+    cudaError_t e_ = (x);                                       \
+    if (e_ != cudaSuccess) {                                    \
+      err = std::string(#x) + ": " + cudaGetErrorString(e_);    \
+      return PGDG_ECUDA;                                        \
+    }                                                           \
+  } while (0)
+
+template <typename T>
+static cudaError_t dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e == cudaSuccess) e = cudaMemset(*p, 0, n * sizeof(T));
+  return e;
+}
+
+template <int D, typename R, bool EX>
+struct Ctx : pgdg_ctx {
+  static constexpr int U = D + 2, B = D + 1, NS = U * D;
+  CaseK K{};
+  DevPtrs<R> P{};
+  std::vector<void*> allocs;
+  int x0b = 0;          /* step-start coordinate buffer (md 1) */
+  double* d_tot = nullptr;
+
+  template <typename T>
+  cudaError_t A(T** p, size_t n) {
+    cudaError_t e = dalloc(p, n);
+    if (e == cudaSuccess) allocs.push_back(*p);
+    return e;
+  }
+
+  ~Ctx() override {
+    if (st) cudaStreamSynchronize(st);
+    for (void* p : allocs) cudaFree(p);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  int init(const pgdg_case* c, int prec, int64_t cap) {
+    cs = *c;
+    precision = prec;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    K.dim = D;
+    for (int d = 0; d < 3; d++) K.N[d] = (d < D) ? cs.ncell[d] : 1;
+    for (int s = 0; s < 6; s++) K.bc[s] = cs.bc[s];
+    K.mgfm_variant = cs.mgfm_variant;
+    K.rad2 = (int)std::ceil(CELL_RATIO / (cs.p_g / cs.p_sz));
+    K.maxpc = (D == 3) ? 64 : 32;
+    K.ncell = (int64_t)K.N[0] * K.N[1] * K.N[2];
+    if (cap <= 0) cap = pgdg_case_num_particles(&cs) * 3 / 2 + 4096;
+    K.cap = cap;
+    K.arena_cap = cap * 32;
+    for (int d = 0; d < 3; d++) {
+      K.bl[d] = cs.box_l[d];
+      K.br[d] = cs.box_r[d];
+      K.ps[d] = cs.p_size[d];
+    }
+    K.p_g = cs.p_g;
+    K.p_sz = cs.p_sz;
+    for (int s = 0; s < F; s++) {
+      K.gamma[s] = cs.gamma[s];
+      K.pinf[s] = cs.pinf[s];
+      K.ini_rho[s] = cs.ini_rho[s];
+    }
+    K.inlet_rho = cs.inlet_rho;
+    for (int d = 0; d < 3; d++) K.inlet_u[d] = cs.inlet_u[d];
+    K.inlet_p = cs.inlet_p;
+    K.cfl = cs.cfl;
+    K.vol_max = powern_d(cs.p_sz, D) * 1.6;
+    K.vol_min = powern_d(cs.p_sz, D) * 2. / 3.;
+    K.dss0 = root_d(K.vol_min, D);
+    for (int i = 0; i < 8; i++)
+      for (int d = 0; d < 3; d++) K.probe[i][d] = cs.probe[i][d];
+    K.bvol = powern_d(cs.p_sz, D - 1);
+    K.brho = cs.ini_rho[0];
+
+    /* particles */
+    const size_t n = (size_t)cap;
+    for (int b = 0; b < 3; b++) CK(A(&P.X[b], D * n));
+    for (int b = 0; b < 2; b++) CK(A(&P.H[b], n));
+    CK(A(&P.vol, n)); CK(A(&P.vol0, n)); CK(A(&P.mass, n)); CK(A(&P.rho, n)); CK(A(&P.E, n));
+    CK(A(&P.c, n)); CK(A(&P.P, n));
+    CK(A(&P.rhov, D * n)); CK(A(&P.v, D * n)); CK(A(&P.tv, D * n));
+    CK(A(&P.sl, NS * n));
+    CK(A(&P.phase, n)); CK(A(&P.mark_in, n)); CK(A(&P.seq, n));
+    CK(A(&P.lcell, n)); CK(A(&P.lkey, n)); CK(A(&P.list_len, n)); CK(A(&P.list_off, n));
+    CK(A(&P.target, n)); CK(A(&P.aff, n)); CK(A(&P.mflag, n)); CK(A(&P.evcode, n));
+    CK(A(&P.scan, n + 1));
+    CK(A(&P.scan_blk, (n + 2047) / 2048 + 2));
+    CK(A(&P.arena, (size_t)K.arena_cap));
+    /* cells */
+    const size_t nc = (size_t)K.ncell;
+    CK(A(&P.crho, F * nc)); CK(A(&P.crhov, F * D * nc)); CK(A(&P.cE, F * nc)); CK(A(&P.cc, F * nc));
+    CK(A(&P.cac, F * nc)); CK(A(&P.calph, F * nc));
+    CK(A(&P.ccoef, F * U * B * nc)); CK(A(&P.ccoef0, F * U * B * nc)); CK(A(&P.cdcoef, F * U * B * nc));
+    CK(A(&P.clim, F * U * nc)); CK(A(&P.cgv, D * D * nc)); CK(A(&P.cv, D * nc)); CK(A(&P.cP, nc));
+    CK(A(&P.cph, F * nc)); CK(A(&P.cphb, F * nc)); CK(A(&P.cused, nc));
+    CK(A(&P.bucket, nc * K.maxpc)); CK(A(&P.bcnt, nc)); CK(A(&P.cflag, nc));
+    CK(A(&P.dirty_q, nc)); CK(A(&P.flag_q, nc));
+    P.qcap = (int64_t)nc;
+    CK(A(&P.cnt, 1));
+    CK(A(&d_tot, 6));
+    P.xb = 0;
+    P.hb = 0;
+    int rc = init_boundary();
+    if (rc) return rc;
+    return init_cells_default();
+  }
+
+  /* boundary particles on the boundary nodes (mpm_ini.cpp:555-620) */
+  int init_boundary() {
+    std::vector<double> bx, bn;
+    const int S2 = (D == 3) ? K.N[2] : 0;
+    for (int sx = 0; sx <= K.N[0]; ++sx)
+      for (int sy = 0; sy <= K.N[1]; ++sy)
+        for (int sz = 0; sz <= S2; ++sz) {
+          bool fg = (sx == 0 || sx == K.N[0] || sy == 0 || sy == K.N[1]);
+          if (D == 3) fg = fg || sz == 0 || sz == K.N[2];
+          if (!fg) continue;
+          double p[3] = {K.bl[0] + K.ps[0] * (sx + 0.), K.bl[1] + K.ps[1] * (sy + 0.), 0.0};
+          if (D == 3) p[2] = K.bl[2] + K.ps[2] * (sz + 0.);
+          double nn[3] = {0, 0, 0};
+          if (sx == 0) nn[0] = -1;
+          else if (sx == K.N[0]) nn[0] = 1;
+          else if (sy == 0) nn[1] = -1;
+          else if (sy == K.N[1]) nn[1] = 1;
+          else if (D == 3 && sz == 0) nn[2] = -1;
+          else if (D == 3 && sz == K.N[2]) nn[2] = 1;
+          for (int d = 0; d < 3; d++) {
+            bx.push_back(p[d]);
+            bn.push_back(nn[d]);
+          }
+        }
+    int64_t nb = (int64_t)bx.size() / 3;
+    K.nbnd = nb;
+    std::vector<R> hx(D * nb), hn(D * nb);
+    std::vector<int32_t> cellof(nb);
+    for (int64_t b = 0; b < nb; b++) {
+      for (int d = 0; d < D; d++) {
+        hx[d * nb + b] = (R)bx[3 * b + d];
+        hn[d * nb + b] = (R)bn[3 * b + d];
+      }
+      int pos[3] = {0, 0, 0};
+      for (int d = 0; d < D; d++) {
+        double q = std::floor((bx[3 * b + d] - K.bl[d]) / K.ps[d]);
+        pos[d] = (!(q >= 0)) ? 0 : (q >= K.N[d] - 1 ? K.N[d] - 1 : (int)q);
+      }
+      cellof[b] = (int32_t)(((int64_t)pos[0] * K.N[1] + pos[1]) * K.N[2] + pos[2]);
+    }
+    std::vector<int32_t> off(K.ncell + 1, 0), ent(nb);
+    for (int64_t b = 0; b < nb; b++) off[cellof[b] + 1]++;
+    for (int64_t c = 0; c < K.ncell; c++) off[c + 1] += off[c];
+    std::vector<int32_t> fill(off.begin(), off.end() - 1);
+    for (int64_t b = 0; b < nb; b++) ent[fill[cellof[b]]++] = (int32_t)b;
+    CK(A(&P.bx, D * nb));
+    CK(A(&P.bn, D * nb));
+    CK(A(&P.boff, K.ncell + 1));
+    CK(A(&P.bent, nb));
+    CK(cudaMemcpy(P.bx, hx.data(), sizeof(R) * D * nb, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.bn, hn.data(), sizeof(R) * D * nb, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.boff, off.data(), sizeof(int32_t) * (K.ncell + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.bent, ent.data(), sizeof(int32_t) * std::max<int64_t>(nb, 1), cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
+
+  int init_cells_default() {
+    /* cells start as MPM::Initialize_case leaves them (mpm_ini.cpp:325-338) */
+    std::vector<double> rho(F * K.ncell), c(F * K.ncell);
+    pgdg_cells v{};
+    v.n = K.ncell;
+    std::vector<double> z3(F * 3 * K.ncell, 0.0), zf(F * K.ncell, 0.0), zc(F * U * B * K.ncell, 0.0),
+        zv(3 * K.ncell, 0.0), zp(K.ncell, 0.0);
+    std::vector<int32_t> ph(F * K.ncell), phb(F * K.ncell), used(K.ncell);
+    std::vector<double> lim(F * U * K.ncell, 1.0);
+    v.rho = rho.data(); v.rhov = z3.data(); v.E = zf.data(); v.c = c.data(); v.ac = nullptr;
+    v.alph = zf.data(); v.coef = zc.data(); v.v = zv.data(); v.P = zp.data();
+    v.ph_state = ph.data(); v.ph_state_b = phb.data(); v.used = used.data(); v.lim_u = lim.data();
+    int rc = pgdg_case_cells(&cs, &v);
+    if (rc) return rc;
+    rc = upload_cells(&v);
+    if (rc) return rc;
+    /* counters */
+    DevCounters h{};
+    h.dt = 0;
+    h.max_v = 1e-7;
+    CK(cudaMemcpy(P.cnt, &h, sizeof(h), cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
+
+  DevCounters counters() {
+    DevCounters h{};
+    cudaStreamSynchronize(st);
+    cudaMemcpy(&h, P.cnt, sizeof(h), cudaMemcpyDeviceToHost);
+    return h;
+  }
+
+  int check() override {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      err = std::string("kernel: ") + cudaGetErrorString(e);
+      return PGDG_ECUDA;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      err = std::string("launch: ") + cudaGetErrorString(e);
+      return PGDG_ECUDA;
+    }
+    DevCounters h = counters();
+    if (h.err) {
+      char b[160];
+      snprintf(b, sizeof(b), "device status 0x%x (1 bucket, 2 list arena, 4 capacity, 8 missing list, 16 cell queue)",
+               h.err);
+      err = b;
+      return (h.err & ERR_NOLIST) ? PGDG_ESTATE : PGDG_EOVERFLOW;
+    }
+    return PGDG_OK;
+  }
+
+  /* ---------------- exchange ---------------- */
+  int upload_particles(const pgdg_particles* pp) override {
+    int64_t n = pp->n;
+    if (n > K.cap) {
+      err = "particle count exceeds capacity";
+      return PGDG_EINVAL;
+    }
+    std::vector<R> x(D * n), v(D * n), tv(D * n), rhov(D * n), sl(NS * n);
+    std::vector<R> vol(n), mass(n), h(n), Pp(n), rho(n), E(n), c(n);
+    std::vector<int8_t> phase(n), mark(n);
+    std::vector<uint64_t> seq(n);
+    std::vector<int32_t> llen(n, 0);
+    std::vector<int64_t> loff(n, 0);
+    uint64_t mx = 0;
+    for (int64_t i = 0; i < n; i++) {
+      for (int d = 0; d < D; d++) {
+        x[d * n + i] = (R)pp->coord[3 * i + d];
+        v[d * n + i] = pp->v ? (R)pp->v[3 * i + d] : R(0);
+        tv[d * n + i] = pp->tv ? (R)pp->tv[3 * i + d] : R(0);
+        rhov[d * n + i] = (R)pp->rhov[3 * i + d];
+      }
+      vol[i] = (R)pp->vol[i]; mass[i] = (R)pp->mass[i]; h[i] = (R)pp->h[i]; Pp[i] = (R)pp->P[i];
+      rho[i] = (R)pp->rho[i]; E[i] = (R)pp->E[i]; c[i] = (R)pp->c[i];
+      for (int t = 0; t < NS; t++) sl[t * n + i] = pp->slope ? (R)pp->slope[NS * i + t] : R(0);
+      phase[i] = (int8_t)pp->phase[i];
+      mark[i] = pp->mark_in ? (int8_t)pp->mark_in[i] : 0;
+      seq[i] = pp->seq ? pp->seq[i] : (uint64_t)i;
+      mx = std::max<uint64_t>(mx, seq[i] + 1);
+    }
+    auto put = [&](R* dst, const std::vector<R>& src, int comps) -> cudaError_t {
+      for (int k = 0; k < comps; k++) {
+        cudaError_t e = cudaMemcpy(dst + (size_t)k * K.cap, src.data() + (size_t)k * n, sizeof(R) * n,
+                                   cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+      }
+      return cudaSuccess;
+    };
+    CK(cudaStreamSynchronize(st));
+    P.xb = 0;
+    P.hb = 0;
+    x0b = 0;
+    CK(put(P.X[0], x, D)); CK(put(P.v, v, D)); CK(put(P.tv, tv, D)); CK(put(P.rhov, rhov, D));
+    CK(put(P.sl, sl, NS));
+    CK(put(P.vol, vol, 1)); CK(put(P.mass, mass, 1)); CK(put(P.H[0], h, 1)); CK(put(P.P, Pp, 1));
+    CK(put(P.rho, rho, 1)); CK(put(P.E, E, 1)); CK(put(P.c, c, 1));
+    CK(cudaMemset(P.phase, 0, K.cap));
+    CK(cudaMemcpy(P.phase, phase.data(), n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.mark_in, mark.data(), n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.seq, seq.data(), 8 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.list_len, llen.data(), 4 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.list_off, loff.data(), 8 * n, cudaMemcpyHostToDevice));
+    DevCounters hc = counters();
+    hc.n_slots = n;
+    hc.n_live = n;
+    hc.seq_next = mx;
+    hc.arena_used = 0;
+    hc.err = 0;
+    hc.n_dirty = hc.n_flagged = 0;
+    CK(cudaMemcpy(P.cnt, &hc, sizeof(hc), cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
+
+  /* alive slots in canonical order */
+  int alive_slots(std::vector<int64_t>& slots) {
+    DevCounters hc = counters();
+    int64_t ns = (int64_t)hc.n_slots;
+    std::vector<int8_t> ph(ns);
+    if (ns) CK(cudaMemcpy(ph.data(), P.phase, ns, cudaMemcpyDeviceToHost));
+    slots.clear();
+    for (int64_t s = 0; s < ns; s++)
+      if (ph[s] != 0) slots.push_back(s);
+    return PGDG_OK;
+  }
+
+  int num_particles(int64_t* n) override {
+    DevCounters hc = counters();
+    *n = (int64_t)hc.n_live;
+    return PGDG_OK;
+  }
+
+  int download_particles(pgdg_particles* pp) override {
+    std::vector<int64_t> slots;
+    int rc = alive_slots(slots);
+    if (rc) return rc;
+    int64_t n = (int64_t)slots.size();
+    if (pp->n < n) {
+      pp->n = n;
+      err = "download capacity too small";
+      return PGDG_EINVAL;
+    }
+    DevCounters hc = counters();
+    int64_t ns = (int64_t)hc.n_slots;
+    auto get = [&](const R* src, int comps, std::vector<R>& dst) -> cudaError_t {
+      dst.resize((size_t)comps * std::max<int64_t>(ns, 1));
+      for (int k = 0; k < comps; k++) {
+        cudaError_t e = cudaMemcpy(dst.data() + (size_t)k * ns, src + (size_t)k * K.cap, sizeof(R) * ns,
+                                   cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return e;
+      }
+      return cudaSuccess;
+    };
+    std::vector<R> x, v, tv, rhov, sl, vol, mass, h, Pp, rho, E, c;
+    CK(get(P.X[P.xb], D, x)); CK(get(P.v, D, v)); CK(get(P.tv, D, tv)); CK(get(P.rhov, D, rhov));
+    CK(get(P.sl, NS, sl)); CK(get(P.vol, 1, vol)); CK(get(P.mass, 1, mass)); CK(get(P.H[P.hb], 1, h));
+    CK(get(P.P, 1, Pp)); CK(get(P.rho, 1, rho)); CK(get(P.E, 1, E)); CK(get(P.c, 1, c));
+    std::vector<int8_t> phase(std::max<int64_t>(ns, 1)), mark(std::max<int64_t>(ns, 1));
+    std::vector<uint64_t> seq(std::max<int64_t>(ns, 1));
+    CK(cudaMemcpy(phase.data(), P.phase, ns, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(mark.data(), P.mark_in, ns, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(seq.data(), P.seq, 8 * ns, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < n; i++) {
+      int64_t s = slots[i];
+      for (int d = 0; d < 3; d++) {
+        bool in = d < D;
+        if (pp->coord) pp->coord[3 * i + d] = in ? (double)x[d * ns + s] : 0.0;
+        if (pp->v) pp->v[3 * i + d] = in ? (double)v[d * ns + s] : 0.0;
+        if (pp->tv) pp->tv[3 * i + d] = in ? (double)tv[d * ns + s] : 0.0;
+        if (pp->rhov) pp->rhov[3 * i + d] = in ? (double)rhov[d * ns + s] : 0.0;
+      }
+      if (pp->vol) pp->vol[i] = vol[s];
+      if (pp->mass) pp->mass[i] = mass[s];
+      if (pp->h) pp->h[i] = h[s];
+      if (pp->P) pp->P[i] = Pp[s];
+      if (pp->rho) pp->rho[i] = rho[s];
+      if (pp->E) pp->E[i] = E[s];
+      if (pp->c) pp->c[i] = c[s];
+      if (pp->slope)
+        for (int t = 0; t < NS; t++) pp->slope[NS * i + t] = sl[t * ns + s];
+      if (pp->phase) pp->phase[i] = phase[s];
+      if (pp->mark_in) pp->mark_in[i] = mark[s];
+      if (pp->seq) pp->seq[i] = seq[s];
+    }
+    pp->n = n;
+    return PGDG_OK;
+  }
+
+  int upload_cells(const pgdg_cells* cc) override {
+    if (cc->n != K.ncell) {
+      err = "cell count mismatch";
+      return PGDG_EINVAL;
+    }
+    const int64_t nc = K.ncell;
+    std::vector<R> rho(F * nc), rhov(F * D * nc), E(F * nc), c(F * nc), ac(F * nc), alph(F * nc),
+        coef(F * U * B * nc), lim(F * U * nc), gv(D * D * nc), v(D * nc), Pp(nc), dco(F * U * B * nc);
+    std::vector<int8_t> ph(F * nc), phb(F * nc), used(nc);
+    for (int64_t ci = 0; ci < nc; ci++) {
+      for (int s = 0; s < F; s++) {
+        int64_t q = ci * F + s;
+        rho[s * nc + ci] = (R)cc->rho[q];
+        for (int d = 0; d < D; d++) rhov[(s * D + d) * nc + ci] = (R)cc->rhov[q * 3 + d];
+        E[s * nc + ci] = (R)cc->E[q];
+        c[s * nc + ci] = (R)cc->c[q];
+        ac[s * nc + ci] = cc->ac ? (R)cc->ac[q] : R(0);
+        alph[s * nc + ci] = (R)cc->alph[q];
+        for (int t = 0; t < U * B; t++) {
+          coef[(s * U * B + t) * nc + ci] = (R)cc->coef[q * U * B + t];
+          dco[(s * U * B + t) * nc + ci] = cc->dcoef ? (R)cc->dcoef[q * U * B + t] : R(0);
+        }
+        for (int u = 0; u < U; u++) lim[(s * U + u) * nc + ci] = cc->lim_u ? (R)cc->lim_u[q * U + u] : R(1);
+        ph[s * nc + ci] = (int8_t)cc->ph_state[q];
+        phb[s * nc + ci] = (int8_t)cc->ph_state_b[q];
+      }
+      for (int d = 0; d < D; d++) v[d * nc + ci] = (R)cc->v[3 * ci + d];
+      Pp[ci] = (R)cc->P[ci];
+      for (int t = 0; t < D * D; t++) gv[t * nc + ci] = cc->g_v ? (R)cc->g_v[ci * D * D + t] : R(0);
+      used[ci] = cc->used ? (int8_t)cc->used[ci] : 1;
+    }
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(P.crho, rho.data(), sizeof(R) * rho.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.crhov, rhov.data(), sizeof(R) * rhov.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cE, E.data(), sizeof(R) * E.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cc, c.data(), sizeof(R) * c.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cac, ac.data(), sizeof(R) * ac.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.calph, alph.data(), sizeof(R) * alph.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.ccoef, coef.data(), sizeof(R) * coef.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cdcoef, dco.data(), sizeof(R) * dco.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.clim, lim.data(), sizeof(R) * lim.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cgv, gv.data(), sizeof(R) * gv.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cv, v.data(), sizeof(R) * v.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cP, Pp.data(), sizeof(R) * Pp.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cph, ph.data(), ph.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cphb, phb.data(), phb.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.cused, used.data(), used.size(), cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
+
+  int download_cells(pgdg_cells* co) override {
+    if (co->n != K.ncell) {
+      err = "cell count mismatch";
+      return PGDG_EINVAL;
+    }
+    const int64_t nc = K.ncell;
+    std::vector<R> rho(F * nc), rhov(F * D * nc), E(F * nc), c(F * nc), ac(F * nc), alph(F * nc),
+        coef(F * U * B * nc), lim(F * U * nc), gv(D * D * nc), v(D * nc), Pp(nc), dco(F * U * B * nc);
+    std::vector<int8_t> ph(F * nc), phb(F * nc), used(nc);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(rho.data(), P.crho, sizeof(R) * rho.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(rhov.data(), P.crhov, sizeof(R) * rhov.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(E.data(), P.cE, sizeof(R) * E.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(c.data(), P.cc, sizeof(R) * c.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ac.data(), P.cac, sizeof(R) * ac.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(alph.data(), P.calph, sizeof(R) * alph.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(coef.data(), P.ccoef, sizeof(R) * coef.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dco.data(), P.cdcoef, sizeof(R) * dco.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(lim.data(), P.clim, sizeof(R) * lim.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(gv.data(), P.cgv, sizeof(R) * gv.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(v.data(), P.cv, sizeof(R) * v.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(Pp.data(), P.cP, sizeof(R) * Pp.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ph.data(), P.cph, ph.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(phb.data(), P.cphb, phb.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(used.data(), P.cused, used.size(), cudaMemcpyDeviceToHost));
+    for (int64_t ci = 0; ci < nc; ci++) {
+      for (int s = 0; s < F; s++) {
+        int64_t q = ci * F + s;
+        if (co->rho) co->rho[q] = rho[s * nc + ci];
+        if (co->rhov) for (int d = 0; d < 3; d++) co->rhov[q * 3 + d] = d < D ? (double)rhov[(s * D + d) * nc + ci] : 0.0;
+        if (co->E) co->E[q] = E[s * nc + ci];
+        if (co->c) co->c[q] = c[s * nc + ci];
+        if (co->ac) co->ac[q] = ac[s * nc + ci];
+        if (co->alph) co->alph[q] = alph[s * nc + ci];
+        if (co->coef) for (int t = 0; t < U * B; t++) co->coef[q * U * B + t] = coef[(s * U * B + t) * nc + ci];
+        if (co->dcoef) for (int t = 0; t < U * B; t++) co->dcoef[q * U * B + t] = dco[(s * U * B + t) * nc + ci];
+        if (co->lim_u) for (int u = 0; u < U; u++) co->lim_u[q * U + u] = lim[(s * U + u) * nc + ci];
+        if (co->ph_state) co->ph_state[q] = ph[s * nc + ci];
+        if (co->ph_state_b) co->ph_state_b[q] = phb[s * nc + ci];
+      }
+      if (co->v) for (int d = 0; d < 3; d++) co->v[3 * ci + d] = d < D ? (double)v[d * nc + ci] : 0.0;
+      if (co->P) co->P[ci] = Pp[ci];
+      if (co->used) co->used[ci] = used[ci];
+      if (co->g_v) for (int t = 0; t < D * D; t++) co->g_v[ci * D * D + t] = gv[t * nc + ci];
+    }
+    return PGDG_OK;
+  }
+
+  int upload_lists(const int64_t* off, const int64_t* ent) override {
+    std::vector<int64_t> slots;
+    int rc = alive_slots(slots);
+    if (rc) return rc;
+    int64_t n = (int64_t)slots.size();
+    DevCounters hc = counters();
+    int64_t ns = (int64_t)hc.n_slots;
+    std::vector<int32_t> len(std::max<int64_t>(ns, 1), -1), arena;
+    std::vector<int64_t> lo(std::max<int64_t>(ns, 1), 0);
+    for (int64_t i = 0; i < n; i++) {
+      int64_t s = slots[i];
+      lo[s] = (int64_t)arena.size();
+      for (int64_t e = off[i]; e < off[i + 1]; e++) {
+        int64_t v = ent[e];
+        if (v >= 0) arena.push_back((int32_t)slots[v]);
+        else if (v == -1) arena.push_back(-1);
+        /* boundary entries are not kept on the device: split/merge never match them */
+      }
+      len[s] = (int32_t)((int64_t)arena.size() - lo[s]);
+    }
+    if ((int64_t)arena.size() > K.arena_cap) {
+      err = "list arena too small";
+      return PGDG_EOVERFLOW;
+    }
+    CK(cudaStreamSynchronize(st));
+    if (!arena.empty()) CK(cudaMemcpy(P.arena, arena.data(), 4 * arena.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.list_len, len.data(), 4 * ns, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.list_off, lo.data(), 8 * ns, cudaMemcpyHostToDevice));
+    hc.arena_used = arena.size();
+    CK(cudaMemcpy(&P.cnt->arena_used, &hc.arena_used, 8, cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
+
+  int download_lists(int64_t* off, int64_t* ent, int32_t* stored, int64_t cap, int64_t* total) override {
+    std::vector<int64_t> slots;
+    int rc = alive_slots(slots);
+    if (rc) return rc;
+    DevCounters hc = counters();
+    int64_t ns = (int64_t)hc.n_slots;
+    std::vector<int32_t> len(std::max<int64_t>(ns, 1));
+    std::vector<int64_t> lo(std::max<int64_t>(ns, 1));
+    std::vector<int32_t> arena(std::max<unsigned long long>(hc.arena_used, 1ull));
+    CK(cudaMemcpy(len.data(), P.list_len, 4 * ns, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(lo.data(), P.list_off, 8 * ns, cudaMemcpyDeviceToHost));
+    if (hc.arena_used) CK(cudaMemcpy(arena.data(), P.arena, 4 * hc.arena_used, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> canon(std::max<int64_t>(ns, 1), -1);
+    for (size_t i = 0; i < slots.size(); i++) canon[slots[i]] = (int64_t)i;
+    int64_t t = 0;
+    for (size_t i = 0; i < slots.size(); i++) {
+      int64_t s = slots[i];
+      if (off) off[i] = t;
+      if (stored) stored[i] = len[s] >= 0 ? 1 : 0;
+      for (int32_t e = 0; e < std::max(len[s], 0); e++) {
+        int32_t q = arena[lo[s] + e];
+        if (ent && t < cap) ent[t] = (q >= 0) ? canon[q] : -1;
+        t++;
+      }
+    }
+    if (off) off[slots.size()] = t;
+    *total = t;
+    return (ent && t > cap) ? PGDG_EOVERFLOW : PGDG_OK;
+  }
+
+  int download_cell_lists(int64_t* off, int64_t* ent, int64_t cap, int64_t* total) override {
+    std::vector<int64_t> slots;
+    int rc = alive_slots(slots);
+    if (rc) return rc;
+    DevCounters hc = counters();
+    int64_t ns = (int64_t)hc.n_slots;
+    std::vector<int32_t> bk(K.ncell * K.maxpc), cnt(K.ncell), boff(K.ncell + 1), bent(std::max<int64_t>(K.nbnd, 1));
+    std::vector<uint32_t> key(std::max<int64_t>(ns, 1));
+    CK(cudaMemcpy(bk.data(), P.bucket, 4 * bk.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cnt.data(), P.bcnt, 4 * cnt.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(boff.data(), P.boff, 4 * boff.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(bent.data(), P.bent, 4 * std::max<int64_t>(K.nbnd, 1), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(key.data(), P.lkey, 4 * ns, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> canon(std::max<int64_t>(ns, 1), -1);
+    for (size_t i = 0; i < slots.size(); i++) canon[slots[i]] = (int64_t)i;
+    int64_t t = 0;
+    for (int64_t c = 0; c < K.ncell; c++) {
+      if (off) off[c] = t;
+      int m = std::min(cnt[c], K.maxpc);
+      int r = 0;
+      for (; r < m && key[bk[c * K.maxpc + r]] < KEY_APPEND; r++) {
+        if (ent && t < cap) ent[t] = canon[bk[c * K.maxpc + r]];
+        t++;
+      }
+      for (int e = boff[c]; e < boff[c + 1]; e++) {
+        if (ent && t < cap) ent[t] = -2 - (int64_t)bent[e];
+        t++;
+      }
+      for (; r < m; r++) {
+        if (ent && t < cap) ent[t] = canon[bk[c * K.maxpc + r]];
+        t++;
+      }
+    }
+    if (off) off[K.ncell] = t;
+    *total = t;
+    return (ent && t > cap) ? PGDG_EOVERFLOW : PGDG_OK;
+  }
+
+  int set_dt(double dt) override {
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(&P.cnt->dt, &dt, 8, cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
+  int set_max_v(double mv) override {
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(&P.cnt->max_v, &mv, 8, cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
+  int capacity(int64_t* c) override {
+    *c = K.cap;
+    return PGDG_OK;
+  }
+  int stats(pgdg_stats* s) override {
+    DevCounters h = counters();
+    std::memset(s, 0, sizeof(*s));
+    s->n_particles = (int64_t)h.n_live;
+    s->n_split = (int64_t)h.n_split;
+    s->n_inlet = (int64_t)h.n_inlet;
+    s->n_outlet = (int64_t)h.n_outlet;
+    s->n_merge = (int64_t)h.n_merge;
+    s->n_affected = (int64_t)h.n_affected;
+    s->mgfm_calls = (int64_t)h.mgfm_calls;
+    s->mgfm_iters = (int64_t)h.mgfm_iters;
+    s->mgfm_maxit_hits = (int64_t)h.mgfm_maxit;
+    s->g2p_fallbacks = (int64_t)h.g2p_fb;
+    s->list_entries = (int64_t)h.arena_used;
+    s->iterate_num = iterate;
+    s->dt = h.dt;
+    s->max_v = h.max_v;
+    return PGDG_OK;
+  }
+
+  /* ---------------- methods ---------------- */
+  int set_timestep(double* dt, double* mv) override {
+    Launch<D, R, EX>::set_timestep(K, P, iterate > 1 ? 1 : 0, st);
+    if (dt || mv) {
+      DevCounters h = counters();
+      if (dt) *dt = h.dt;
+      if (mv) *mv = h.max_v;
+    }
+    return PGDG_OK;
+  }
+  int used_state() override {
+    Launch<D, R, EX>::used_state(K, P, st);
+    return PGDG_OK;
+  }
+  int bin() override {
+    Launch<D, R, EX>::bin(K, P, st);
+    return PGDG_OK;
+  }
+  int split() override {
+    Launch<D, R, EX>::split(K, P, st);
+    return PGDG_OK;
+  }
+  int merge() override {
+    Launch<D, R, EX>::merge(K, P, st);
+    return PGDG_OK;
+  }
+  /* flag 4: a cell's particle list is its bucket and a particle's in_ele[0]
+   * is the cell holding it (lcell); both are kept current by bin/split/merge */
+  int refresh_membership() override { return PGDG_OK; }
+  /* flag 2: the lists are recomputed from the stage-start coordinates inside
+   * the shifting kernel; nothing to do here */
+  int refresh_neighbors() override { return PGDG_OK; }
+  int p2g() override {
+    Launch<D, R, EX>::p2g(K, P, st);
+    return PGDG_OK;
+  }
+  int limiter() override {
+    Launch<D, R, EX>::limiter(K, P, st);
+    return PGDG_OK;
+  }
+  int grid_acc() override {
+    Launch<D, R, EX>::grid_acc(K, P, st);
+    return PGDG_OK;
+  }
+  int update_grid(int md) override {
+    Launch<D, R, EX>::update_grid(K, P, md, st);
+    return PGDG_OK;
+  }
+  int update_particle(int md) override {
+    const int xs = P.xb, hs = P.hb, hn = 1 - P.hb;
+    int x0, xn;
+    if (md == 0) {
+      x0 = xs;
+      xn = (xs + 1) % 3;
+      x0b = xs;
+    } else {
+      x0 = x0b;
+      xn = 3 - xs - x0b;
+      if (xn == xs || xn == x0 || xn < 0 || xn > 2) xn = (xs + 1) % 3;  /* md 1 without md 0 */
+    }
+    Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, st);
+    Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, st);
+    if (md == 1) Launch<D, R, EX>::store_lists(K, P, xs, hs, xn, st);
+    P.xb = xn;
+    P.hb = hn;
+    return PGDG_OK;
+  }
+  int run_step(int64_t n) override {
+    if (n == 1) used_state();
+    bin();
+    split();
+    for (int it = 0; it < cs.merge_iters; it++) merge();
+    refresh_membership();
+    for (int md = 0; md < 2; md++) {
+      refresh_neighbors();
+      if (md == 0) p2g();
+      limiter();
+      grid_acc();
+      update_grid(md);
+      update_particle(md);
+    }
+    return PGDG_OK;
+  }
+  int advance(int nsteps) override {
+    for (int s = 0; s < nsteps; s++) {
+      set_timestep(nullptr, nullptr);
+      iterate++;
+      run_step(iterate);
+    }
+    return PGDG_OK;
+  }
+  int totals(double* out) override {
+    Launch<D, R, EX>::totals(K, P, d_tot, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(out, d_tot, 6 * sizeof(double), cudaMemcpyDeviceToHost));
+    return PGDG_OK;
+  }
+};
+
+}  // namespace
+
+/* ---------------------------------------------------------------------- */
+extern "C" {
+
+int pgdg_create(const pgdg_case* cs, int precision, int64_t capacity, pgdg_ctx** out) {
+  if (!cs || !out || cs->nfld != 2 || (cs->dim != 2 && cs->dim != 3)) return PGDG_EINVAL;
+  if (precision != PGDG_PREC_FP64 && precision != PGDG_PREC_MIXED && precision != PGDG_PREC_FP64_FMA)
+    return PGDG_EINVAL;
+  int dev = 0;
+  if (cudaGetDeviceCount(&dev) != cudaSuccess || dev < 1) return PGDG_ECUDA;
+  pgdg_ctx* c;
+  int rc;
+#define PGDG_MK(DD, RR, XX)                 \
+  {                                         \
+    auto* x = new Ctx<DD, RR, XX>();        \
+    rc = x->init(cs, precision, capacity);  \
+    c = x;                                  \
+  }
+  if (cs->dim == 2) {
+    if (precision == PGDG_PREC_FP64) PGDG_MK(2, double, true)
+    else if (precision == PGDG_PREC_FP64_FMA) PGDG_MK(2, double, false)
+    else PGDG_MK(2, float, false)
+  } else {
+    if (precision == PGDG_PREC_FP64) PGDG_MK(3, double, true)
+    else if (precision == PGDG_PREC_FP64_FMA) PGDG_MK(3, double, false)
+    else PGDG_MK(3, float, false)
+  }
+#undef PGDG_MK
+  if (rc) {
+    fprintf(stderr, "pgdg_create: %s\n", c->err.c_str());
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return PGDG_OK;
+}
+int pgdg_destroy(pgdg_ctx* ctx) {
+  delete ctx;
+  return PGDG_OK;
+}
+const char* pgdg_last_error(pgdg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+int pgdg_capacity(pgdg_ctx* ctx, int64_t* cap) { return ctx->capacity(cap); }
+int pgdg_upload_particles(pgdg_ctx* ctx, const pgdg_particles* p) { return ctx->upload_particles(p); }
+int pgdg_download_particles(pgdg_ctx* ctx, pgdg_particles* p) { return ctx->download_particles(p); }
+int pgdg_num_particles(pgdg_ctx* ctx, int64_t* n) { return ctx->num_particles(n); }
+int pgdg_upload_cells(pgdg_ctx* ctx, const pgdg_cells* c) { return ctx->upload_cells(c); }
+int pgdg_download_cells(pgdg_ctx* ctx, pgdg_cells* c) { return ctx->download_cells(c); }
+int pgdg_upload_lists(pgdg_ctx* ctx, const int64_t* off, const int64_t* ent) { return ctx->upload_lists(off, ent); }
+int pgdg_download_lists(pgdg_ctx* ctx, int64_t* off, int64_t* ent, int32_t* stored, int64_t cap, int64_t* total) {
+  return ctx->download_lists(off, ent, stored, cap, total);
+}
+int pgdg_download_cell_lists(pgdg_ctx* ctx, int64_t* off, int64_t* ent, int64_t cap, int64_t* total) {
+  return ctx->download_cell_lists(off, ent, cap, total);
+}
+int pgdg_set_dt(pgdg_ctx* ctx, double dt) { return ctx->set_dt(dt); }
+int pgdg_set_iterate(pgdg_ctx* ctx, int64_t n) {
+  ctx->iterate = n;
+  return PGDG_OK;
+}
+int pgdg_set_max_v(pgdg_ctx* ctx, double mv) { return ctx->set_max_v(mv); }
+int pgdg_set_seed_mode(pgdg_ctx* ctx, int mode) {
+  ctx->seed_mode = mode;
+  return PGDG_OK;
+}
+int pgdg_get_stats(pgdg_ctx* ctx, pgdg_stats* st) { return ctx->stats(st); }
+int pgdg_synchronize(pgdg_ctx* ctx) { return ctx->check(); }
+int pgdg_set_timestep(pgdg_ctx* ctx, double* dt, double* mv) { return ctx->set_timestep(dt, mv); }
+int pgdg_used_state_update(pgdg_ctx* ctx) { return ctx->used_state(); }
+int pgdg_bin_particles(pgdg_ctx* ctx) { return ctx->bin(); }
+int pgdg_split_particle_fast(pgdg_ctx* ctx) { return ctx->split(); }
+int pgdg_merge_particle_fast(pgdg_ctx* ctx) { return ctx->merge(); }
+int pgdg_refresh_membership(pgdg_ctx* ctx) { return ctx->refresh_membership(); }
+int pgdg_refresh_neighbors(pgdg_ctx* ctx) { return ctx->refresh_neighbors(); }
+int pgdg_mls_p2g(pgdg_ctx* ctx) { return ctx->p2g(); }
+int pgdg_calculate_limiter(pgdg_ctx* ctx) { return ctx->limiter(); }
+int pgdg_grid_acceleration(pgdg_ctx* ctx) { return ctx->grid_acc(); }
+int pgdg_update_grid(pgdg_ctx* ctx, int md) { return ctx->update_grid(md); }
+int pgdg_update_particle(pgdg_ctx* ctx, int md) { return ctx->update_particle(md); }
+int pgdg_run_step(pgdg_ctx* ctx, int64_t n) { return ctx->run_step(n); }
+int pgdg_advance(pgdg_ctx* ctx, int nsteps) { return ctx->advance(nsteps); }
+int pgdg_totals(pgdg_ctx* ctx, double* out6) { return ctx->totals(out6); }
+
+}  // extern "C"

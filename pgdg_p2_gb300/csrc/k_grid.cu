@@ -1,0 +1,910 @@
+/*
+ * k_grid.cu -- grid kernels of the step: Used_state_update, Set_timestep,
+ * MLS_P2G, Calculate_limiter, Grid_acceleration (DG volume + face residual with
+ * the MGFM ghost state), Update_grid and the conservation totals.
+ *
+ * One thread per cell; cell fields are component-major (field[t * ncell + ci])
+ * so a warp's loads of one field are coalesced.  R is float (mixed precision) or
+ * double (plain FP64 path); the MGFM Newton solve and the P2G moment sums are
+ * FP64 in both.
+ */
+#include "pgdg_dev.cuh"
+
+namespace pgdg {
+
+constexpr int BLK = 256;
+#define GRID_STRIDE(i, n) for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); \
+                               i += (int64_t)gridDim.x * blockDim.x)
+
+template <int D>
+__device__ __forceinline__ void cijk(const CaseK& K, int64_t ci, int* idx) {
+  idx[2] = (int)(ci % K.N[2]);
+  idx[1] = (int)((ci / K.N[2]) % K.N[1]);
+  idx[0] = (int)(ci / ((int64_t)K.N[1] * K.N[2]));
+}
+__device__ __forceinline__ int64_t cidx3(const CaseK& K, int i, int j, int k) {
+  return ((int64_t)i * K.N[1] + j) * K.N[2] + k;
+}
+/* cell centre box_l + p_size (idx + 0.5) (mpm_ini.cpp:305-311) */
+template <int D>
+__device__ __forceinline__ void center(const CaseK& K, const int* idx, double* xc) {
+  for (int d = 0; d < 3; d++) xc[d] = (d < D) ? K.bl[d] + K.ps[d] * (idx[d] + 0.5) : 0.0;
+}
+
+/* Cell_dg face f (mpm_ini.cpp:447-545): order yL, xR, yR, xL, zL, zR */
+struct FaceK {
+  int axis;       /* normal axis */
+  double sgn;     /* normal = sgn e_axis */
+  double cen[3], t0[3], t1[3], S;
+  int bound;
+  int nb[3];
+};
+template <int D>
+__device__ __forceinline__ void face(const CaseK& K, const int* idx, const double* xc, int f, FaceK& fc) {
+  const double px = K.ps[0], py = K.ps[1], pz = K.ps[2];
+  for (int d = 0; d < 3; d++) { fc.cen[d] = xc[d]; fc.t0[d] = 0; fc.t1[d] = 0; fc.nb[d] = idx[d]; }
+  int side;
+  switch (f) {
+    case 0: fc.axis = 1; fc.sgn = -1; fc.t0[0] = 0.5 * px; fc.t1[2] = 0.5 * pz; fc.cen[1] = xc[1] - 0.5 * py;
+      fc.S = (D == 3) ? px * pz : px; fc.nb[1] -= 1; side = 2; break;
+    case 1: fc.axis = 0; fc.sgn = 1; fc.t0[1] = 0.5 * py; fc.t1[2] = 0.5 * pz; fc.cen[0] = xc[0] + 0.5 * px;
+      fc.S = (D == 3) ? py * pz : py; fc.nb[0] += 1; side = 1; break;
+    case 2: fc.axis = 1; fc.sgn = 1; fc.t0[0] = -0.5 * px; fc.t1[2] = 0.5 * pz; fc.cen[1] = xc[1] + 0.5 * py;
+      fc.S = (D == 3) ? px * pz : px; fc.nb[1] += 1; side = 3; break;
+    case 3: fc.axis = 0; fc.sgn = -1; fc.t0[1] = -0.5 * py; fc.t1[2] = 0.5 * pz; fc.cen[0] = xc[0] - 0.5 * px;
+      fc.S = (D == 3) ? py * pz : py; fc.nb[0] -= 1; side = 0; break;
+    case 4: fc.axis = 2; fc.sgn = -1; fc.t0[0] = 0.5 * px; fc.t1[1] = 0.5 * py; fc.cen[2] = xc[2] - 0.5 * pz;
+      fc.S = py * px; fc.nb[2] -= 1; side = 4; break;
+    default: fc.axis = 2; fc.sgn = 1; fc.t0[0] = 0.5 * px; fc.t1[1] = 0.5 * py; fc.cen[2] = xc[2] + 0.5 * pz;
+      fc.S = py * px; fc.nb[2] += 1; side = 5; break;
+  }
+  if (D == 2) fc.t1[2] = 0;
+  bool inside = true;
+  for (int d = 0; d < D; d++) inside = inside && fc.nb[d] >= 0 && fc.nb[d] < K.N[d];
+  fc.bound = inside ? 0 : K.bc[side];
+}
+
+/* ------------------------------------------------------------------ */
+/* Used_state_update (mpm.cpp:184-263)                                */
+/* ------------------------------------------------------------------ */
+template <int D, typename R, bool EX>
+__global__ void k_used_mark(CaseK K, DevPtrs<R> P, int8_t* tmp) {
+  const int64_t nc = K.ncell;
+  GRID_STRIDE(ci, nc) {
+    if (!(P.cph[ci] == 1 || P.cph[nc + ci] == 1)) continue;
+    int idx[3];
+    cijk<D>(K, ci, idx);
+    const int Ib[3] = {5, 5, D == 3 ? 5 : 0};
+    for (int t = max(idx[0] - Ib[0], 0); t <= min(idx[0] + Ib[0], K.N[0] - 1); t++)
+      for (int s = max(idx[1] - Ib[1], 0); s <= min(idx[1] + Ib[1], K.N[1] - 1); s++)
+        for (int q = max(idx[2] - Ib[2], 0); q <= min(idx[2] + Ib[2], K.N[2] - 1); q++) tmp[cidx3(K, t, s, q)] = 1;
+  }
+}
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::used_state(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
+  cudaMemsetAsync(P.cused, 0, K.ncell, st);
+  k_used_mark<D, R, EX><<<grid_for(K.ncell, BLK), BLK, 0, st>>>(K, P, P.cused);
+}
+
+/* ------------------------------------------------------------------ */
+/* Set_timestep (mpm.cpp:19-57, particle.cpp:554-569)                 */
+/* ------------------------------------------------------------------ */
+template <typename T>
+__device__ __forceinline__ T warp_min(T v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <typename R, bool EX>
+__global__ void k_dt_init(DevPtrs<R> P) {
+  P.cnt->dt_bits = (unsigned long long)__double_as_longlong(1.e20);
+  P.cnt->maxv_bits = 0ull;
+}
+
+template <int D, typename R, bool EX>
+__global__ void k_dt_reduce(CaseK K, DevPtrs<R> P, int by_cells) {
+  double tmin = 1.e20, vmax = 0.0;
+  if (by_cells) {
+    const int64_t nc = K.ncell;
+    const R hh = R(CELL_RATIO / CUT_OFF * K.p_sz);
+    const R ds = hh / R(CELL_RATIO) * R(CUT_OFF);
+    GRID_STRIDE(ci, nc) {
+      if (!P.cused[ci]) continue;
+      R sq = P.cv[ci] * P.cv[ci];
+      for (int k = 1; k < D; k++) sq = sq + P.cv[k * nc + ci] * P.cv[k * nc + ci];
+      R U = rsqrt_<R>(sq);
+      R c12 = amax1(P.cc[ci], P.cc[nc + ci]);
+      R a12 = amax1(P.cac[ci], P.cac[nc + ci]);
+      R t = R(K.cfl) * ds / (c12 + U);
+      R tmp = R(K.cfl) * rsqrt_<R>(ds / a12);
+      t = amin1(t, tmp);
+      tmin = fmin(tmin, (double)t);
+      vmax = fmax(vmax, (double)U);
+    }
+  } else {
+    const int64_t n = (int64_t)P.cnt->n_slots;
+    const R* H = P.H[P.hb];
+    GRID_STRIDE(p, n) {
+      if (P.phase[p] == 0) continue;
+      R sq = P.v[p] * P.v[p];
+      for (int k = 1; k < D; k++) sq = sq + P.v[k * K.cap + p] * P.v[k * K.cap + p];
+      R U = rsqrt_<R>(sq);
+      R ds = H[p] / R(CELL_RATIO) * R(CUT_OFF);
+      R c12 = amax1(P.c[p], R(0));
+      R t = R(K.cfl) * ds / (c12 + U);
+      tmin = fmin(tmin, (double)t);
+      vmax = fmax(vmax, (double)U);
+    }
+  }
+  tmin = warp_min(tmin);
+  vmax = warp_max(vmax);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&P.cnt->dt_bits, (unsigned long long)__double_as_longlong(tmin));
+    atomicMax(&P.cnt->maxv_bits, (unsigned long long)__double_as_longlong(vmax));
+  }
+}
+
+template <typename R, bool EX>
+__global__ void k_dt_final(DevPtrs<R> P) {
+  P.cnt->dt = __longlong_as_double((long long)P.cnt->dt_bits);
+  P.cnt->max_v = __longlong_as_double((long long)P.cnt->maxv_bits);
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::set_timestep(const CaseK& K, const DevPtrs<R>& P, int by_cells, cudaStream_t st) {
+  k_dt_init<R, EX><<<1, 1, 0, st>>>(P);
+  k_dt_reduce<D, R, EX><<<grid_for(by_cells ? K.ncell : K.cap, BLK), BLK, 0, st>>>(K, P, by_cells);
+  k_dt_final<R, EX><<<1, 1, 0, st>>>(P);
+}
+
+/* ------------------------------------------------------------------ */
+/* MLS_P2G (mpm.cpp:274-382)                                          */
+/* ------------------------------------------------------------------ */
+template <int D, typename R>
+__device__ __forceinline__ R kernel_w_r(R dist, R h, R C) {
+  R s = dist / h;
+  R val = R(0);
+  if (s < R(2)) {
+    R q = R(1.) - R(0.5) * s;
+    val = C * (((q * q) * q) * q) * (R(1.) + R(2.) * s);
+  }
+  return val;
+}
+
+template <int D, typename R, bool EX>
+__global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
+  constexpr int U = D + 2, B = D + 1, NS = U * D;
+  const int64_t nc = K.ncell;
+  const R* X = P.X[P.xb];
+  const double hi = K.p_g * 1 * 3.2 / CUT_OFF;
+  const double cut = 1.5 * K.p_sz;
+  const float lo2 = (float)(cut * cut * (1.0 - 1e-5)), hi2 = (float)(cut * cut * (1.0 + 1e-5));
+  GRID_STRIDE(ci, nc) {
+    if (!P.cused[ci]) continue;
+    int idx[3];
+    cijk<D>(K, ci, idx);
+    double xc[3];
+    center<D>(K, idx, xc);
+    R xcr[3];
+    for (int d = 0; d < 3; d++) xcr[d] = (R)xc[d];
+    int lo[3], hi3[3];
+    for (int d = 0; d < 3; d++) {
+      lo[d] = max(idx[d] - 1, 0);
+      hi3[d] = min(idx[d] + 1, (d < D ? K.N[d] : 1) - 1);
+    }
+    double mass_t[F] = {0, 0};
+    int newmask = 0;
+    for (int pass = 0; pass < 2; pass++) {
+      double p_avg[U], Cf[NS];
+      int want = -1;
+      if (pass == 1) {
+        for (int s = 0; s < F; s++) {
+          bool ph = mass_t[s] > 0;
+          if (ph && P.cphb[s * nc + ci] == 0) newmask |= 1 << s;
+        }
+        if (!newmask) break;
+        /* newly present phases are rare; sum their averages one phase at a time */
+      }
+      for (int sw = 0; sw < (pass == 0 ? 1 : F); sw++) {
+        if (pass == 1) {
+          if (!(newmask & (1 << sw))) continue;
+          want = sw;
+          for (int u = 0; u < U; u++) p_avg[u] = 0;
+          for (int t = 0; t < NS; t++) Cf[t] = 0;
+        }
+        for (int t = lo[0]; t <= hi3[0]; t++)
+          for (int s = lo[1]; s <= hi3[1]; s++)
+            for (int m = lo[2]; m <= hi3[2]; m++) {
+              int64_t cn = cidx3(K, t, s, m);
+              int cntq = min(P.bcnt[cn], K.maxpc);
+              const int32_t* bk = P.bucket + cn * K.maxpc;
+              for (int r = 0; r < cntq; r++) {
+                int32_t q = bk[r];
+                int ph = P.phase[q] - 1;
+                if (pass == 1 && ph != want) continue;
+                R xij[3];
+                for (int d = 0; d < D; d++) xij[d] = X[d * K.cap + q] - xcr[d];
+                bool in;
+                double dist;
+                if (sizeof(R) == 4) {
+                  float dd = 0.f;
+                  for (int d = 0; d < D; d++) dd += (float)xij[d] * (float)xij[d];
+                  if (dd < lo2) in = true;
+                  else if (dd > hi2) in = false;
+                  else {
+                    double e2 = 0;
+                    for (int d = 0; d < D; d++) {
+                      double t2 = (double)X[d * K.cap + q] - xc[d];
+                      e2 = (d == 0) ? t2 * t2 : e2 + t2 * t2;
+                    }
+                    in = sqrt(e2) < cut;
+                  }
+                  dist = (double)sqrtf(dd);
+                } else {
+                  double e2 = 0;
+                  for (int d = 0; d < D; d++) {
+                    double t2 = (double)xij[d];
+                    e2 = (d == 0) ? t2 * t2 : e2 + t2 * t2;
+                  }
+                  dist = sqrt(e2);
+                  in = dist < cut;
+                }
+                if (!in) continue;
+                R ww = kernel_w_r<D, R>((R)dist, (R)hi, (R)Cw) * P.vol[q];
+                if (ph < 0 || ph >= F) continue;
+                if (pass == 0) {
+                  mass_t[ph] += (double)ww;
+                } else {
+                  double wwd = (double)ww;
+                  double pj[U];
+                  pj[0] = (double)P.rho[q];
+                  for (int k = 0; k < D; k++) pj[1 + k] = (double)P.rhov[k * K.cap + q];
+                  pj[U - 1] = (double)P.E[q];
+                  for (int u = 0; u < U; u++) {
+                    double acc = 0;
+                    for (int b = 0; b < D; b++) {
+                      double sv = (double)P.sl[(u * D + b) * K.cap + q];
+                      acc = (b == 0) ? sv * (-(double)xij[b]) : acc + sv * (-(double)xij[b]);
+                    }
+                    pj[u] += acc;
+                  }
+                  for (int u = 0; u < U; u++) p_avg[u] += pj[u] * wwd;
+                  for (int tt = 0; tt < NS; tt++) Cf[tt] += (double)P.sl[tt * K.cap + q] * wwd;
+                }
+              }
+            }
+        if (pass == 1) {
+          /* initialise the newly present phase (mpm.cpp:345-363) */
+          const int ss = want;
+          const double mt = mass_t[ss] + 1e-20;
+          for (int u = 0; u < U; u++) p_avg[u] /= mt;
+          for (int t = 0; t < NS; t++) Cf[t] /= mt;
+          for (int u = 0; u < U; u++)
+            for (int b = 0; b < B; b++) P.ccoef[((ss * U + u) * B + b) * nc + ci] = R(0);
+          P.ccoef[((ss * U + 0) * B + 0) * nc + ci] = (R)p_avg[0];
+          P.crho[ss * nc + ci] = (R)p_avg[0];
+          for (int k = 0; k < D; k++) {
+            P.ccoef[((ss * U + 1 + k) * B + 0) * nc + ci] = (R)p_avg[1 + k];
+            P.crhov[(ss * D + k) * nc + ci] = (R)p_avg[1 + k];
+          }
+          P.ccoef[((ss * U + U - 1) * B + 0) * nc + ci] = (R)p_avg[U - 1];
+          P.cE[ss * nc + ci] = (R)p_avg[U - 1];
+          for (int u = 0; u < U; u++)
+            for (int b = 0; b < D; b++) P.ccoef[((ss * U + u) * B + 1 + b) * nc + ci] = (R)Cf[u * D + b];
+          R rho = P.crho[ss * nc + ci];
+          R sq = R(0);
+          for (int k = 0; k < D; k++) {
+            R rv = P.crhov[(ss * D + k) * nc + ci];
+            P.cv[k * nc + ci] = rv / rho;
+            sq = (k == 0) ? rv * rv : sq + rv * rv;
+          }
+          R e_j = P.cE[ss * nc + ci] - R(0.5) * sq / rho;
+          P.cP[ci] = eos_p<R>(e_j, (R)K.gamma[ss], (R)K.pinf[ss]);
+          for (int t = 0; t < U * B; t++) P.ccoef0[(ss * U * B + t) * nc + ci] = P.ccoef[(ss * U * B + t) * nc + ci];
+        }
+      }
+    }
+    double mass_total = 0;
+    for (int t = 0; t < F; t++) mass_total += mass_t[t];
+    for (int ss = 0; ss < F; ss++) {
+      int ph = mass_t[ss] > 0 ? 1 : 0;
+      P.cph[ss * nc + ci] = (int8_t)ph;
+      P.calph[ss * nc + ci] = (R)(mass_t[ss] / (mass_total + 1e-20));
+      P.cphb[ss * nc + ci] = (int8_t)ph;
+      if (ph == 0) {
+        for (int t = 0; t < U * B; t++) {
+          P.ccoef[(ss * U * B + t) * nc + ci] = R(0);
+          P.ccoef0[(ss * U * B + t) * nc + ci] = R(0);
+        }
+        P.crho[ss * nc + ci] = (R)K.ini_rho[ss];
+        for (int k = 0; k < D; k++) P.crhov[(ss * D + k) * nc + ci] = R(0);
+      }
+    }
+  }
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::p2g(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
+  const double hi = K.p_g * 1 * 3.2 / CUT_OFF;
+  double hh = (D == 2) ? hi * hi : hi * hi * hi;
+  double Cw = (D == 2) ? 1.0 / PI_REF / hh * 7. / 4. : 1.0 / PI_REF / hh * 21. / 16.;
+  k_p2g<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, Cw);
+}
+
+/* ------------------------------------------------------------------ */
+/* Calculate_limiter (mpm.cpp:392-738)                                */
+/* ------------------------------------------------------------------ */
+template <typename R>
+__device__ __forceinline__ R limiter_fn(R ds, int bd_fg) {
+  /* Limiter (glbfunc.h:283-299) */
+  R val = R(1);
+  if (ds > R(0) && ds < R(0.5)) val = R(2) * ds;
+  else if (ds >= R(0.5)) val = R(1);
+  if (bd_fg == 1) val = (fabs(ds) + ds) / (fabs(ds) + R(1));
+  return val;
+}
+
+template <int D, typename R, bool EX>
+__global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
+  constexpr int U = D + 2, B = D + 1, NF = 2 * D;
+  const int64_t nc = K.ncell;
+  GRID_STRIDE(ci, nc) {
+    if (!P.cused[ci]) continue;
+    int idx[3];
+    cijk<D>(K, ci, idx);
+    double xc[3];
+    center<D>(K, idx, xc);
+    R u_max[F][U], u_min[F][U], pi[F][U], lim[F][U];
+    for (int s = 0; s < F; s++)
+      for (int u = 0; u < U; u++) {
+        u_max[s][u] = R(-1e20);
+        u_min[s][u] = R(1e20);
+        lim[s][u] = R(1.);
+      }
+    for (int s = 0; s < F; s++) {
+      pi[s][0] = P.crho[s * nc + ci];
+      for (int k = 0; k < D; k++) pi[s][1 + k] = P.crhov[(s * D + k) * nc + ci];
+      pi[s][U - 1] = P.cE[s * nc + ci];
+    }
+    /* G_v (mpm.cpp:469-533) */
+    int bd_fg = 0;
+    R vc[3];
+    for (int k = 0; k < D; k++) vc[k] = P.cv[k * nc + ci];
+    for (int dd = 0; dd < D; dd++) {
+      R pd = (R)K.ps[dd];
+      if (idx[dd] == K.N[dd] - 1) {
+        for (int r = 0; r < D; r++) P.cgv[(r * D + dd) * nc + ci] = ((dd == 0 ? vc[r] : R(0)) - vc[r]) / (R(0.5) * pd);
+        bd_fg = 1;
+      } else if (idx[dd] == 0) {
+        for (int r = 0; r < D; r++) P.cgv[(r * D + dd) * nc + ci] = (vc[r] - (dd == 0 ? vc[r] : R(0))) / (R(0.5) * pd);
+        bd_fg = 1;
+      } else {
+        int a[3] = {idx[0], idx[1], idx[2]}, b[3] = {idx[0], idx[1], idx[2]};
+        a[dd] += 1;
+        b[dd] -= 1;
+        int64_t cR = cidx3(K, a[0], a[1], a[2]), cL = cidx3(K, b[0], b[1], b[2]);
+        for (int r = 0; r < D; r++) P.cgv[(r * D + dd) * nc + ci] = (P.cv[r * nc + cR] - P.cv[r * nc + cL]) / (R(2) * pd);
+      }
+    }
+    const bool mirror_j = (idx[1] == K.N[1] - 1 || idx[1] == 0);
+    const bool mirror_k = (D == 3) && (idx[2] == K.N[2] - 1 || idx[2] == 0);
+    for (int f = 0; f < NF; f++) {
+      FaceK fc;
+      face<D>(K, idx, xc, f, fc);
+      if (fc.bound == 0) {
+        int64_t nb = cidx3(K, fc.nb[0], fc.nb[1], fc.nb[2]);
+        for (int s = 0; s < F; s++) {
+          R pj[U];
+          for (int u = 0; u < U; u++) pj[u] = R(0);
+          for (int s1 = 0; s1 < F; s1++) {
+            R aj = P.calph[s1 * nc + nb];
+            if (aj == R(0)) continue;
+            R rhoj = P.crho[s1 * nc + nb];
+            R rvj[3];
+            for (int k = 0; k < D; k++) rvj[k] = P.crhov[(s1 * D + k) * nc + nb];
+            R Ej = P.cE[s1 * nc + nb];
+            if (s1 != s) {
+              R vj[3], sq = R(0);
+              for (int k = 0; k < D; k++) {
+                vj[k] = rvj[k] / rhoj;
+                sq = (k == 0) ? vj[k] * vj[k] : sq + vj[k] * vj[k];
+              }
+              R rhoe_j = Ej - R(0.5) * rhoj * sq;
+              R P_j = eos_p<R>(rhoe_j, (R)K.gamma[s1], (R)K.pinf[s1]);
+              rhoj = P.crho[s * nc + ci];
+              for (int k = 0; k < D; k++) rvj[k] = rhoj * vj[k];
+              Ej = eos_rhoe<R>(P_j, (R)K.gamma[s], (R)K.pinf[s]) + R(0.5) * rhoj * sq;
+            }
+            pj[0] += rhoj * aj;
+            for (int k = 0; k < D; k++) pj[1 + k] += rvj[k] * aj;
+            pj[U - 1] += Ej * aj;
+          }
+          for (int u = 0; u < U; u++) {
+            R d = pj[u] - pi[s][u];
+            u_max[s][u] = amax1(u_max[s][u], d);
+            u_min[s][u] = amin1(u_min[s][u], d);
+          }
+        }
+      } else {
+        for (int s = 0; s < F; s++) {
+          R pj[U];
+          pj[0] = P.crho[s * nc + ci];
+          for (int k = 0; k < D; k++) pj[1 + k] = P.crhov[(s * D + k) * nc + ci];
+          pj[U - 1] = P.cE[s * nc + ci];
+          if (fc.bound == PGDG_BC_INLET || fc.bound == PGDG_BC_OUTLET || fc.bound == PGDG_BC_TRANSMISSIVE)
+            for (int u = 0; u < U; u++) pj[u] = pi[s][u];
+          if (fc.bound != PGDG_BC_TRANSMISSIVE) {
+            if (mirror_j) pj[2] = -P.crhov[(s * D + 1) * nc + ci];
+            if (mirror_k) pj[3] = -P.crhov[(s * D + 2) * nc + ci];
+          }
+          for (int u = 0; u < U; u++) {
+            R d = pj[u] - pi[s][u];
+            u_max[s][u] = amax1(u_max[s][u], d);
+            u_min[s][u] = amin1(u_min[s][u], d);
+          }
+        }
+      }
+    }
+    for (int s = 0; s < F; s++)
+      for (int u = 0; u < U; u++) {
+        u_max[s][u] = amax1(u_max[s][u], R(0.));
+        u_min[s][u] = amin1(u_min[s][u], R(0.));
+      }
+    for (int f = 0; f < NF; f++) {
+      FaceK fc;
+      face<D>(K, idx, xc, f, fc);
+      R dr[3];
+      if (fc.bound == 0) {
+        double xn[3];
+        center<D>(K, fc.nb, xn);
+        for (int d = 0; d < D; d++) dr[d] = (R)(xn[d] - xc[d]);
+      } else {
+        for (int d = 0; d < D; d++) dr[d] = (R)(fc.cen[d] - xc[d]);
+      }
+      for (int s = 0; s < F; s++) {
+        int lim_fg = bd_fg;
+        if (P.calph[s * nc + ci] != R(1)) lim_fg = 1;
+        for (int u = 0; u < U; u++) {
+          R dU = R(0);
+          for (int b = 0; b < D; b++) {
+            R cf = P.ccoef[((s * U + u) * B + 1 + b) * nc + ci];
+            dU = (b == 0) ? cf * dr[b] : dU + cf * dr[b];
+          }
+          R sd = R(1);
+          if (dU >= R(0)) sd = limiter_fn<R>(fabs(u_max[s][u] / (dU + R(1e-20))), lim_fg);
+          else if (dU < R(0)) sd = limiter_fn<R>(fabs(u_min[s][u] / (dU + R(1e-20))), lim_fg);
+          lim[s][u] = amin1(lim[s][u], sd);
+        }
+      }
+    }
+    /* positivity probe (mpm.cpp:690-728) */
+    const int NPR = (D == 3) ? 8 : 4;
+    for (int s = 0; s < F; s++) {
+      const R gs = (R)K.gamma[s], pf = (R)K.pinf[s];
+      int fg = 0;
+      for (int pr = 0; pr < NPR && !fg; pr++) {
+        R Ui[U];
+        for (int u = 0; u < U; u++) {
+          R acc = R(0);
+          for (int b = 0; b < D; b++) {
+            R cf = P.ccoef[((s * U + u) * B + 1 + b) * nc + ci];
+            acc = (b == 0) ? cf * (R)K.probe[pr][b] : acc + cf * (R)K.probe[pr][b];
+          }
+          Ui[u] = P.ccoef[((s * U + u) * B) * nc + ci] + lim[s][u] * acc;
+        }
+        R sq = Ui[1] * Ui[1];
+        for (int k = 1; k < D; k++) sq = sq + Ui[1 + k] * Ui[1 + k];
+        R e_p = Ui[U - 1] - R(0.5) * sq / Ui[0];
+        R P_p = eos_p<R>(e_p, gs, pf);
+        if (P_p < R(-0.05) * pf || Ui[0] < R(0)) fg = 1;
+      }
+      for (int u = 0; u < U; u++) P.clim[(s * U + u) * nc + ci] = fg ? R(0.) : lim[s][u];
+    }
+  }
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::limiter(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
+  k_limiter<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P);
+}
+
+/* ------------------------------------------------------------------ */
+/* Grid_acceleration (particle_flow.cpp:16-405)                       */
+/* ------------------------------------------------------------------ */
+template <int D, typename R>
+struct Prim {
+  R U[D + 2];
+  R v[3];
+  R P, c, vn;
+};
+
+/* normal-column flux F[u] = DF[u][a] with DF = U v^T + P I (+ v P in the energy row) */
+template <int D, typename R>
+__device__ __forceinline__ void flux_col(const R* Uu, const R* v, R Pp, int a, R* Fc) {
+  constexpr int U = D + 2;
+  for (int u = 0; u < U; u++) Fc[u] = Uu[u] * v[a];
+  Fc[1 + a] += Pp;
+  Fc[U - 1] += v[a] * Pp;
+}
+
+template <int D, typename R, bool EX>
+__global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int variant, double voli_d,
+                                                 double mij1, double mij2, double mij3) {
+  constexpr int U = D + 2, B = D + 1, NF = 2 * D, NQ = (D == 3) ? 4 : 2, NG = (D == 3) ? 8 : 4;
+  const int64_t nc = K.ncell;
+  const double gp[2] = {-1. / sqrt(3.), 1. / sqrt(3.)};
+  unsigned long long ncall = 0, nit = 0, nmax = 0;
+  GRID_STRIDE(ci, nc) {
+    if (!P.cused[ci]) continue;
+    int idx[3];
+    cijk<D>(K, ci, idx);
+    double xc[3];
+    center<D>(K, idx, xc);
+    const bool mirror_j = (idx[1] == K.N[1] - 1 || idx[1] == 0);
+    const bool mirror_k = (D == 3) && (idx[2] == K.N[2] - 1 || idx[2] == 0);
+    for (int ss = 0; ss < F; ss++) {
+      if (P.cph[ss * nc + ci] != 1) continue;
+      const R gs = (R)K.gamma[ss], pfs = (R)K.pinf[ss];
+      R co[U][B], L[U], dc[U][B];
+      for (int u = 0; u < U; u++) {
+        for (int b = 0; b < B; b++) {
+          co[u][b] = P.ccoef[((ss * U + u) * B + b) * nc + ci];
+          dc[u][b] = R(0);
+        }
+        L[u] = P.clim[(ss * U + u) * nc + ci];
+      }
+      /* volume integral, 2^D Gauss points */
+      const R voli = (R)voli_d;
+      for (int g = 0; g < NG; g++) {
+        int g1 = (D == 3) ? (g >> 2) : (g >> 1), g2 = (D == 3) ? ((g >> 1) & 1) : (g & 1), g3 = g & 1;
+        R dp[3] = {(R)(gp[g1] * (K.ps[0] / 2)), (R)(gp[g2] * (K.ps[1] / 2)), (D == 3) ? (R)(gp[g3] * (K.ps[2] / 2)) : R(0)};
+        const R gw = (D == 3) ? R(0.125) : R(0.25);
+        R Up[U];
+        for (int u = 0; u < U; u++) {
+          R acc = co[u][1] * dp[0];
+          for (int b = 1; b < D; b++) acc = acc + co[u][1 + b] * dp[b];
+          Up[u] = co[u][0] + L[u] * acc;
+        }
+        R rho_p = Up[0];
+        R vp[3], sq = Up[1] * Up[1];
+        for (int k = 1; k < D; k++) sq = sq + Up[1 + k] * Up[1 + k];
+        for (int k = 0; k < D; k++) vp[k] = Up[1 + k] / rho_p;
+        R P_p = eos_p<R>(Up[U - 1] - R(0.5) * sq / rho_p, gs, pfs);
+        for (int bi = 1; bi <= D; bi++) {
+          R Fc[U];
+          flux_col<D, R>(Up, vp, P_p, bi - 1, Fc);
+          for (int u = 0; u < U; u++) dc[u][bi] += Fc[u] * gw * voli;
+        }
+      }
+      /* face integral */
+      for (int f = 0; f < NF; f++) {
+        FaceK fc;
+        face<D>(K, idx, xc, f, fc);
+        const int a = fc.axis;
+        const R na = (R)fc.sgn;
+        R DFn[B][U];
+        for (int b = 0; b < B; b++)
+          for (int u = 0; u < U; u++) DFn[b][u] = R(0);
+        int64_t nb = -1;
+        if (fc.bound == 0) nb = cidx3(K, fc.nb[0], fc.nb[1], fc.nb[2]);
+        double xn[3] = {0, 0, 0};
+        if (nb >= 0) center<D>(K, fc.nb, xn);
+        for (int qd = 0; qd < NQ; qd++) {
+          int g1 = (D == 3) ? (qd >> 1) : qd, g2 = qd & 1;
+          double dpv[3];
+          for (int d = 0; d < 3; d++) dpv[d] = (D == 3) ? gp[g1] * fc.t0[d] + gp[g2] * fc.t1[d] : gp[g1] * fc.t0[d];
+          const R gw = (D == 3) ? R(0.25) : R(0.5);
+          R dri[3];
+          for (int d = 0; d < D; d++) dri[d] = (R)(dpv[d] + fc.cen[d] - xc[d]);
+          R Ui[U];
+          for (int u = 0; u < U; u++) {
+            R acc = co[u][1] * dri[0];
+            for (int b = 1; b < D; b++) acc = acc + co[u][1 + b] * dri[b];
+            Ui[u] = co[u][0] + L[u] * acc;
+          }
+          const R rho_i = Ui[0], E_i = Ui[U - 1];
+          R v_i[3], sq = Ui[1] * Ui[1];
+          for (int k = 1; k < D; k++) sq = sq + Ui[1 + k] * Ui[1 + k];
+          for (int k = 0; k < D; k++) v_i[k] = Ui[1 + k] / rho_i;
+          const R P_i = eos_p<R>(E_i - R(0.5) * sq / rho_i, gs, pfs);
+          const R c_i = rsqrt_<R>(gs * (pfs + P_i) / rho_i);
+          const R vni = v_i[a] * na;
+          R Fi[U];
+          flux_col<D, R>(Ui, v_i, P_i, a, Fi);
+          R Nb[B];
+          Nb[0] = R(1.);
+          for (int d = 0; d < D; d++) Nb[1 + d] = dri[d];
+          if (fc.bound == 0) {
+            for (int s1 = 0; s1 < F; s1++) {
+              const R aj = P.calph[s1 * nc + nb];
+              if (aj == R(0)) continue;
+              R drj[3];
+              for (int d = 0; d < D; d++) drj[d] = (R)(dpv[d] + fc.cen[d] - xn[d]);
+              R Uj[U];
+              for (int u = 0; u < U; u++) {
+                R acc = P.ccoef[((s1 * U + u) * B + 1) * nc + nb] * drj[0];
+                for (int b = 1; b < D; b++) acc = acc + P.ccoef[((s1 * U + u) * B + 1 + b) * nc + nb] * drj[b];
+                Uj[u] = P.ccoef[((s1 * U + u) * B) * nc + nb] + P.clim[(s1 * U + u) * nc + nb] * acc;
+              }
+              R rho_j = Uj[0], E_j = Uj[U - 1];
+              R v_j[3], rhov_j[3];
+              R sqj = R(0);
+              for (int k = 0; k < D; k++) {
+                rhov_j[k] = Uj[1 + k];
+                v_j[k] = rhov_j[k] / rho_j;
+                sqj = (k == 0) ? v_j[k] * v_j[k] : sqj + v_j[k] * v_j[k];
+              }
+              R rhoe_j = E_j - R(0.5) * sqj * rho_j;
+              R P_j = eos_p<R>(rhoe_j, (R)K.gamma[s1], (R)K.pinf[s1]);
+              R vnj = v_j[a] * na;
+              if (ss != s1) {
+                double gh[3];
+                int it = mgfm((double)vni, (double)vnj, (double)P_i, (double)P_j, (double)rho_i, (double)rho_j,
+                              K.gamma[ss], K.pinf[ss], K.gamma[s1], K.pinf[s1], variant, -1.0, gh);
+                ncall++;
+                nit += it;
+                if (it >= 50) nmax++;
+                rho_j = (R)gh[0];
+                P_j = (R)gh[1];
+                vnj = (R)gh[2];
+                sqj = R(0);
+                for (int k = 0; k < D; k++) {
+                  v_j[k] = v_i[k] - (k == a ? vni * na : R(0)) + (k == a ? vnj * na : R(0));
+                  rhov_j[k] = rho_j * v_j[k];
+                  sqj = (k == 0) ? v_j[k] * v_j[k] : sqj + v_j[k] * v_j[k];
+                }
+                E_j = eos_rhoe<R>(P_j, gs, pfs) + R(0.5) * rho_j * sqj;
+              }
+              const R c_j = rsqrt_<R>(gs * (pfs + P_j) / rho_j);
+              R Ujj[U];
+              Ujj[0] = rho_j;
+              for (int k = 0; k < D; k++) Ujj[1 + k] = rhov_j[k];
+              Ujj[U - 1] = E_j;
+              R Fj[U];
+              flux_col<D, R>(Ujj, v_j, P_j, a, Fj);
+              const R vni2 = v_i[a] * na;
+              vnj = v_j[a] * na;
+              /* HLLC (particle_flow.cpp:232-272) */
+              const R SL = amin1(vni2 - c_i, vnj - c_j);
+              const R SR = amax1(vni2 + c_i, vnj + c_j);
+              const R S_s = ((P_j - P_i) + rho_i * vni2 * (SL - vni2) - rho_j * vnj * (SR - vnj)) /
+                            (rho_i * (SL - vni2) - rho_j * (SR - vnj));
+              R Fh[U];
+              if (SL > R(0)) {
+                for (int u = 0; u < U; u++) Fh[u] = Fi[u];
+              } else if (SL <= R(0) && S_s >= R(0)) {
+                const R rho_sL = rho_i * (SL - vni2) / (SL - S_s);
+                R UsL[U];
+                UsL[0] = rho_sL;
+                for (int k = 0; k < D; k++) UsL[1 + k] = rho_sL * (v_i[k] + (k == a ? (S_s - vni2) * na : R(0)));
+                UsL[U - 1] = rho_sL * (E_i / rho_i + (S_s - vni2) * (S_s + P_i / (rho_i * (SL - vni2))));
+                for (int u = 0; u < U; u++) Fh[u] = Fi[u] + SL * (UsL[u] - Ui[u]) * na;
+              } else if (S_s <= R(0) && SR >= R(0)) {
+                const R rho_sR = rho_j * (SR - vnj) / (SR - S_s);
+                R UsR[U];
+                UsR[0] = rho_sR;
+                for (int k = 0; k < D; k++) UsR[1 + k] = rho_sR * (v_j[k] + (k == a ? (S_s - vnj) * na : R(0)));
+                UsR[U - 1] = rho_sR * (E_j / rho_j + (S_s - vnj) * (S_s + P_j / (rho_j * (SR - vnj))));
+                for (int u = 0; u < U; u++) Fh[u] = Fj[u] + SR * (UsR[u] - Ujj[u]) * na;
+              } else if (SR <= R(0)) {
+                for (int u = 0; u < U; u++) Fh[u] = Fj[u];
+              } else {
+                for (int u = 0; u < U; u++) Fh[u] = R(0);
+              }
+              for (int b = 0; b < B; b++)
+                for (int u = 0; u < U; u++) DFn[b][u] += Fh[u] * Nb[b] * gw * aj;
+            }
+          } else if (fc.bound == PGDG_BC_WALL) {
+            for (int b = 0; b < B; b++) DFn[b][1 + a] += P_i * Nb[b] * gw;
+          } else {
+            R rho_j = rho_i, P_j = P_i, E_j = E_i;
+            R v_j[3], rhov_j[3];
+            for (int k = 0; k < D; k++) {
+              v_j[k] = v_i[k];
+              rhov_j[k] = rho_j * v_j[k];
+            }
+            if (fc.bound == PGDG_BC_INLET) {
+              rho_j = (R)K.inlet_rho;
+              R sqj = R(0);
+              for (int k = 0; k < D; k++) {
+                v_j[k] = (R)K.inlet_u[k];
+                rhov_j[k] = rho_j * v_j[k];
+                sqj = (k == 0) ? v_j[k] * v_j[k] : sqj + v_j[k] * v_j[k];
+              }
+              P_j = (R)K.inlet_p;
+              E_j = eos_rhoe<R>(P_j, gs, pfs) + R(0.5) * sqj * rho_j;
+            }
+            if (fc.bound != PGDG_BC_TRANSMISSIVE) {
+              if (mirror_j) {
+                v_j[1] = -v_i[1];
+                for (int k = 0; k < D; k++) rhov_j[k] = rho_j * v_j[k];
+              }
+              if (mirror_k) {
+                v_j[2] = -v_i[2];
+                for (int k = 0; k < D; k++) rhov_j[k] = rho_j * v_j[k];
+              }
+            }
+            R Uj[U];
+            Uj[0] = rho_j;
+            for (int k = 0; k < D; k++) Uj[1 + k] = rhov_j[k];
+            Uj[U - 1] = E_j;
+            const R c_j = rsqrt_<R>(gs * (pfs + P_j) / rho_j);
+            const R vnj = v_j[a] * na;
+            R Fj[U];
+            flux_col<D, R>(Uj, v_j, P_j, a, Fj);
+            const R SL = amin1(vni - c_i, vnj - c_j);
+            const R SR = amax1(vni + c_i, vnj + c_j);
+            R Fh[U];
+            if (SL > R(0)) {
+              for (int u = 0; u < U; u++) Fh[u] = Fi[u];
+            } else if (SL <= R(0) && SR >= R(0)) {
+              for (int u = 0; u < U; u++) Fh[u] = (SR * Fi[u] - SL * Fj[u] + SL * SR * (Uj[u] - Ui[u]) * na) / (SR - SL);
+            } else if (SR < R(0)) {
+              for (int u = 0; u < U; u++) Fh[u] = Fj[u];
+            } else {
+              for (int u = 0; u < U; u++) Fh[u] = R(0);
+            }
+            for (int b = 0; b < B; b++)
+              for (int u = 0; u < U; u++) DFn[b][u] += Fh[u] * Nb[b] * gw;
+          }
+        }
+        const R Sj = (R)fc.S;
+        for (int b = 0; b < B; b++)
+          for (int u = 0; u < U; u++) dc[u][b] += (-DFn[b][u] * na) * Sj;
+      }
+      const R inv[4] = {R(1. / (voli_d + 1e-20)), R(1. / (mij1 + 1e-20)), R(1. / (mij2 + 1e-20)),
+                        R(1. / (mij3 + 1e-20))};
+      for (int u = 0; u < U; u++)
+        for (int b = 0; b < B; b++) P.cdcoef[((ss * U + u) * B + b) * nc + ci] = dc[u][b] * inv[b];
+    }
+  }
+  if (ncall) {
+    atomicAdd(&P.cnt->mgfm_calls, ncall);
+    atomicAdd(&P.cnt->mgfm_iters, nit);
+    if (nmax) atomicAdd(&P.cnt->mgfm_maxit, nmax);
+  }
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::grid_acc(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
+  double voli = K.ps[0] * K.ps[1];
+  if (D == 3) voli = voli * K.ps[2];
+  double ps[3] = {K.ps[0] / 2, K.ps[1] / 2, K.ps[2] / 2};
+  double m1 = (ps[0] * ps[0] / 3.) * voli, m2 = (ps[1] * ps[1] / 3.) * voli, m3 = (ps[2] * ps[2] / 3.) * voli;
+  k_grid_acc<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, m1, m2, m3);
+}
+
+/* ------------------------------------------------------------------ */
+/* Update_grid (mpm.cpp:768-830)                                      */
+/* ------------------------------------------------------------------ */
+template <int D, typename R, bool EX>
+__global__ void k_update_grid(CaseK K, DevPtrs<R> P, int md) {
+  constexpr int U = D + 2, B = D + 1;
+  const int64_t nc = K.ncell;
+  const R dt = (R)P.cnt->dt;
+  GRID_STRIDE(ci, nc) {
+    if (!P.cused[ci]) continue;
+    R rhov_a[3] = {0, 0, 0}, rho_a = 0, P_a = 0;
+    R vcur[3];
+    for (int k = 0; k < D; k++) vcur[k] = P.cv[k * nc + ci];
+    R Pc = P.cP[ci];
+    for (int s = 0; s < F; s++) {
+      R c_s = 0, ac_s = 0;
+      for (int t = 0; t < U; t++) {
+        R l = fabs(P.clim[(s * U + t) * nc + ci]);
+        for (int b = 1; b < B; b++) {
+          int64_t o = ((s * U + t) * B + b) * nc + ci;
+          P.cdcoef[o] *= l;
+          P.ccoef[o] *= l;
+        }
+      }
+      const R alph = P.calph[s * nc + ci];
+      if (P.cph[s * nc + ci] == 1) {
+        for (int t = 0; t < U * B; t++) {
+          int64_t o = (s * U * B + t) * nc + ci;
+          R co = P.ccoef[o], d = P.cdcoef[o];
+          if (md == 0) {
+            P.ccoef0[o] = co;
+            P.ccoef[o] = co + d * dt;
+          } else {
+            P.ccoef[o] = R(0.5) * (d * dt + co + P.ccoef0[o]);
+          }
+        }
+        R rho = P.ccoef[((s * U) * B) * nc + ci];
+        P.crho[s * nc + ci] = rho;
+        R sq = R(0);
+        for (int k = 0; k < D; k++) {
+          R rv = P.ccoef[((s * U + 1 + k) * B) * nc + ci];
+          P.crhov[(s * D + k) * nc + ci] = rv;
+          sq = (k == 0) ? rv * rv : sq + rv * rv;
+        }
+        R E = P.ccoef[((s * U + U - 1) * B) * nc + ci];
+        P.cE[s * nc + ci] = E;
+        Pc = eos_p<R>(E - R(0.5) * sq / rho, (R)K.gamma[s], (R)K.pinf[s]);
+        c_s = rsqrt_<R>((R)K.gamma[s] * ((R)K.pinf[s] + Pc) / rho);
+        R d00 = P.cdcoef[((s * U) * B) * nc + ci];
+        R asq = R(0);
+        for (int k = 0; k < D; k++) {
+          R ak = (P.cdcoef[((s * U + 1 + k) * B) * nc + ci] - d00 * vcur[k]) / rho;
+          asq = (k == 0) ? ak * ak : asq + ak * ak;
+        }
+        ac_s = rsqrt_<R>(asq);
+      }
+      P.cc[s * nc + ci] = c_s;
+      P.cac[s * nc + ci] = ac_s;
+      for (int k = 0; k < D; k++) rhov_a[k] += P.crhov[(s * D + k) * nc + ci] * alph;
+      rho_a += P.crho[s * nc + ci] * alph;
+      P_a += Pc * alph;
+    }
+    for (int k = 0; k < D; k++) P.cv[k * nc + ci] = rhov_a[k] / rho_a;
+    P.cP[ci] = P_a;
+  }
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::update_grid(const CaseK& K, const DevPtrs<R>& P, int md, cudaStream_t st) {
+  k_update_grid<D, R, EX><<<grid_for(K.ncell, BLK), BLK, 0, st>>>(K, P, md);
+}
+
+/* ------------------------------------------------------------------ */
+/* conservation totals (Triple_point_2phase/mpm_ini.cpp:599-654)       */
+/* ------------------------------------------------------------------ */
+template <int D, typename R, bool EX>
+__global__ void k_totals(CaseK K, DevPtrs<R> P, double* out) {
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const int64_t n = (int64_t)P.cnt->n_slots;
+  GRID_STRIDE(p, n) {
+    int ph = P.phase[p];
+    if (ph == 0) continue;
+    double m = (double)P.rho[p] * (double)P.vol[p];
+    acc[ph - 1] += m;
+    acc[2] += (double)P.E[p] * (double)P.vol[p];
+  }
+  const int64_t nc = K.ncell;
+  double voli = K.ps[0] * K.ps[1] * (D == 3 ? K.ps[2] : 1.0);
+  GRID_STRIDE(ci, nc) {
+    if (!P.cused[ci]) continue;
+    for (int s = 0; s < F; s++) {
+      if (P.cph[s * nc + ci] != 1) continue;
+      double a = (double)P.calph[s * nc + ci];
+      acc[3 + s] += voli * a * (double)P.crho[s * nc + ci];
+      acc[5] += voli * a * (double)P.cE[s * nc + ci];
+    }
+  }
+  for (int k = 0; k < 6; k++) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&out[k], v);
+  }
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out6, cudaStream_t st) {
+  cudaMemsetAsync(d_out6, 0, 6 * sizeof(double), st);
+  k_totals<D, R, EX><<<grid_for(K.cap > K.ncell ? K.cap : K.ncell, BLK), BLK, 0, st>>>(K, P, d_out6);
+}
+
+#define PGDG_INST(D, R, EX)                                                                     \
+  template void Launch<D, R, EX>::used_state(const CaseK&, const DevPtrs<R>&, cudaStream_t);       \
+  template void Launch<D, R, EX>::set_timestep(const CaseK&, const DevPtrs<R>&, int, cudaStream_t); \
+  template void Launch<D, R, EX>::p2g(const CaseK&, const DevPtrs<R>&, cudaStream_t);              \
+  template void Launch<D, R, EX>::limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \
+  template void Launch<D, R, EX>::grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);         \
+  template void Launch<D, R, EX>::update_grid(const CaseK&, const DevPtrs<R>&, int, cudaStream_t); \
+  template void Launch<D, R, EX>::totals(const CaseK&, const DevPtrs<R>&, double*, cudaStream_t);
+#ifdef PGDG_EXACT_TU
+PGDG_INST(2, double, true)
+PGDG_INST(3, double, true)
+#else
+PGDG_INST(2, double, false)
+PGDG_INST(3, double, false)
+PGDG_INST(2, float, false)
+PGDG_INST(3, float, false)
+#endif
+
+}  // namespace pgdg

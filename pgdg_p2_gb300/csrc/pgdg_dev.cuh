@@ -1,0 +1,199 @@
+/*
+ * pgdg_dev.cuh -- device state of one context and the launch interface between
+ * the host driver (capi.cu) and the kernel translation units.
+ *
+ * Layout in HBM (structure of arrays, component-major so that a warp reading
+ * one field of consecutive particles or cells is coalesced):
+ *   particles  field[t * cap + slot]   slots in canonical (particle_fluid) order;
+ *              new particles are appended, removed ones become tombstones
+ *              (phase 0) until compaction
+ *   cells      field[t * ncell + ci]   ci = (i * NY + j) * NZ + k
+ *   buckets    bucket[ci * maxpc + r]  the Cell_list of every cell (fluid slots
+ *              in list order) with count bcnt[ci]
+ */
+#ifndef PGDG_DEV_CUH
+#define PGDG_DEV_CUH
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "../../include/pgdg_types.h"
+#include "pgdg_math.cuh"
+
+namespace pgdg {
+
+constexpr int F = 2;
+/* list-order keys (Cell_list order): base entries are ordered by slot,
+ * appended entries (Add_particle during split/merge) by an append counter */
+constexpr uint32_t KEY_APPEND = 0x80000000u;
+
+/* error bits */
+enum : uint32_t {
+  ERR_BUCKET = 1u << 0,    /* a cell bucket overflowed */
+  ERR_ARENA = 1u << 1,     /* neighbour-list arena overflowed */
+  ERR_CAPACITY = 1u << 2,  /* particle slot capacity exceeded */
+  ERR_NOLIST = 1u << 3,    /* split/merge needed a list the device did not keep */
+  ERR_CELLQ = 1u << 4,     /* flagged-cell queue overflowed */
+  ERR_QUEUE = 1u << 5,     /* interface queue overflowed */
+};
+
+struct DevCounters {
+  unsigned long long n_slots;     /* slots in use (live + tombstones) */
+  unsigned long long n_live;
+  unsigned long long seq_next;
+  unsigned long long append_next; /* Add_particle counter within a step */
+  unsigned long long arena_used;
+  unsigned long long n_dirty, n_flagged;
+  unsigned long long n_split, n_inlet, n_outlet, n_merge, n_affected;
+  unsigned long long step_split, step_new, step_surv;
+  unsigned long long mgfm_calls, mgfm_iters, mgfm_maxit, g2p_fb;
+  unsigned long long dt_bits, maxv_bits; /* atomic min/max scratch */
+  unsigned long long queue_n;
+  unsigned int err;
+  unsigned int pad;
+  double dt, max_v;
+};
+
+/* case constants handed to kernels by value */
+struct CaseK {
+  int dim;
+  int N[3];
+  int bc[6];
+  int mgfm_variant;
+  int rad2;          /* flag-2 scan radius in cells (level_infor.cpp:155) */
+  int maxpc;
+  int64_t ncell;
+  int64_t cap;
+  int64_t nbnd;
+  int64_t arena_cap;
+  double bl[3], br[3], ps[3];
+  double p_g, p_sz;
+  double gamma[F], pinf[F], ini_rho[F];
+  double inlet_rho, inlet_u[3], inlet_p;
+  double cfl;
+  double vol_max, vol_min, dss0;
+  double probe[8][3];
+  double bvol, brho;
+};
+
+/* device pointers; R is the storage/arithmetic type of the stage fields */
+template <typename R>
+struct DevPtrs {
+  /* particles */
+  R* X[3];          /* rotating coordinate buffers, each D*cap */
+  R* H[2];          /* ping-pong smoothing length */
+  R *vol, *vol0, *mass, *rho, *E, *c, *P;
+  R *rhov, *v, *tv; /* D*cap */
+  R* sl;            /* U*D*cap: coef[0] columns 1..D */
+  int8_t* phase;    /* 0 = tombstone */
+  int8_t* mark_in;
+  uint64_t* seq;
+  int32_t* lcell;   /* Cell_list the slot is in (-1 none) */
+  uint32_t* lkey;   /* order inside that list */
+  int32_t* list_len;/* stored neighbour list (-1: not kept) */
+  int64_t* list_off;
+  int32_t* target;  /* merge partner (copy_p[0]) */
+  uint8_t* aff;     /* affected (needs a fresh flag-3 list) */
+  uint8_t* mflag;   /* merge role: 1 survivor, 2 removed */
+  int8_t* evcode;   /* split event code */
+  unsigned long long* scan;  /* cap+1 prefix buffer */
+  unsigned long long* scan_blk;
+  int32_t* arena;
+  /* boundary particles */
+  R *bx, *bn;       /* D*nbnd */
+  int32_t *boff, *bent;  /* per-cell CSR of boundary particles */
+  /* cells */
+  R *crho, *crhov, *cE, *cc, *cac, *calph;  /* F, F*D, F, F, F, F */
+  R *ccoef, *ccoef0, *cdcoef;                /* F*U*B */
+  R *clim;                                   /* F*U */
+  R *cgv;                                    /* D*D */
+  R *cv;                                     /* D */
+  R* cP;
+  int8_t *cph, *cphb, *cused;                /* F, F, 1 */
+  int32_t *bucket, *bcnt;
+  uint32_t* cflag;  /* bit0 dirty bucket, bit1 flagged (affected neighbourhood) */
+  int32_t *dirty_q, *flag_q;
+  int64_t qcap;     /* capacity of dirty_q / flag_q */
+  DevCounters* cnt;
+  int xb;           /* index of the current coordinate buffer */
+  int hb;           /* index of the current h buffer */
+};
+
+/* ---------------- cell ids ---------------- */
+template <int D>
+__device__ __forceinline__ int64_t cidx(const CaseK& K, const int* pos) {
+  return ((int64_t)pos[0] * K.N[1] + (D > 1 ? pos[1] : 0)) * K.N[2] + (D > 2 ? pos[2] : 0);
+}
+
+/* get_cell_id (glbfunc.h:161-173) in FP64 */
+template <int D>
+__device__ void cell_pos_exact(const CaseK& K, const double* x, int* pos) {
+  pos[0] = pos[1] = pos[2] = 0;
+  for (int d = 0; d < D; d++) {
+    double q = floor(ddiv(dsub(x[d], K.bl[d]), K.ps[d]));
+    int ip;
+    if (!(q >= 0)) ip = 0;
+    else if (q >= K.N[d] - 1) ip = K.N[d] - 1;
+    else ip = (int)q;
+    pos[d] = ip;
+  }
+}
+
+/* the same cell id from stored coordinates; in FP32 storage a float quotient
+ * decides unless it lies within a relative 1e-6 of an integer */
+template <int D, typename R>
+__device__ void cell_pos(const CaseK& K, const R* xr, int* pos) {
+  if (sizeof(R) == 4) {
+    bool ok = true;
+    pos[0] = pos[1] = pos[2] = 0;
+    for (int d = 0; d < D; d++) {
+      float qf = ((float)xr[d] - (float)K.bl[d]) / (float)K.ps[d];
+      float fl = floorf(qf);
+      float fr = qf - fl;
+      float m = 1e-6f * (fabsf(qf) + 16.f);
+      if (!(fr >= m && fr <= 1.f - m)) ok = false;
+      int ip;
+      if (!(fl >= 0.f)) ip = 0;
+      else if (fl >= (float)(K.N[d] - 1)) ip = K.N[d] - 1;
+      else ip = (int)fl;
+      pos[d] = ip;
+    }
+    if (ok) return;
+  }
+  double xd[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) xd[d] = (double)xr[d];
+  cell_pos_exact<D>(K, xd, pos);
+}
+
+/* ---------------- host-side launch interface ---------------- */
+/* EX = true: exact-order FP64 build (no FMA contraction), bit-identical to the oracle */
+template <int D, typename R, bool EX>
+struct Launch {
+  /* k_particles.cu */
+  static void bin(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  static void split(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  static void merge(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  static void store_lists(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, cudaStream_t);
+  static void reset_lists(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  /* k_grid.cu */
+  static void used_state(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  static void set_timestep(const CaseK&, const DevPtrs<R>&, int by_cells, cudaStream_t);
+  static void p2g(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  static void limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  static void grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  static void update_grid(const CaseK&, const DevPtrs<R>&, int md, cudaStream_t);
+  static void totals(const CaseK&, const DevPtrs<R>&, double* d_out6, cudaStream_t);
+  /* k_g2p.cu */
+  /* xs/hs: stage-start coordinate/h buffers, x0: step-start coordinates (md 1),
+   * xn/hn: buffers receiving the new coordinates/h */
+  static void g2p(const CaseK&, const DevPtrs<R>&, int md, int xs, int x0, int xn, int hn, cudaStream_t);
+  static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, cudaStream_t);
+};
+
+/* shared helpers used by several translation units */
+int grid_for(int64_t n, int block);
+void scan_u64(unsigned long long* data, unsigned long long* blk, const unsigned long long* d_n, int64_t cap,
+              cudaStream_t st);
+
+}  // namespace pgdg
+#endif

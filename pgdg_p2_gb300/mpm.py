@@ -1,0 +1,250 @@
+"""Host-side mirror of the reference's MPM method set over libpgdg_gpu.so.
+
+`MPM` wraps one device context and exposes the methods the 3D_generalized
+driver calls (3D_generalized/PGDG_3D_spheric/mpm.h:160-194) under the same
+names: Set_timestep, Used_state_update, Map_the_particle_to_tree,
+Split_particle_fast, Merge_particle_fast, MLS_P2G, Calculate_limiter,
+Grid_acceleration, Update_grid, Update_particle and MPM_run_simulation.  Every
+call goes through the C ABI in include/pgdg.h; a failing call raises PgdgError
+with the library's error text.  There is no CPU fallback: without the CUDA
+library or a GPU, construction fails.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+from .abi import (PREC_FP64, PREC_MIXED, SEED_MLP, SEED_PLAIN, Cells, Particles, PgdgError,  # noqa: F401
+                  check, declare_case_builder, pgdg_case, pgdg_cells, pgdg_particles, pgdg_stats)
+
+_lib = None
+
+
+def lib():
+    """Load (building first if needed) the in-tree libpgdg_gpu.so."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path) or os.environ.get("PGDG_REBUILD"):
+            path = _build.build()
+        L = C.CDLL(path)
+        P = C.POINTER
+        vp = C.c_void_p
+        declare_case_builder(L)
+        L.pgdg_create.argtypes = [P(pgdg_case), C.c_int, C.c_int64, P(vp)]
+        L.pgdg_last_error.argtypes = [vp]
+        L.pgdg_last_error.restype = C.c_char_p
+        for name in ("pgdg_destroy", "pgdg_used_state_update", "pgdg_bin_particles", "pgdg_split_particle_fast",
+                     "pgdg_merge_particle_fast", "pgdg_refresh_membership", "pgdg_refresh_neighbors",
+                     "pgdg_mls_p2g", "pgdg_calculate_limiter", "pgdg_grid_acceleration", "pgdg_synchronize"):
+            getattr(L, name).argtypes = [vp]
+        L.pgdg_capacity.argtypes = [vp, P(C.c_int64)]
+        L.pgdg_upload_particles.argtypes = [vp, P(pgdg_particles)]
+        L.pgdg_download_particles.argtypes = [vp, P(pgdg_particles)]
+        L.pgdg_num_particles.argtypes = [vp, P(C.c_int64)]
+        L.pgdg_upload_cells.argtypes = [vp, P(pgdg_cells)]
+        L.pgdg_download_cells.argtypes = [vp, P(pgdg_cells)]
+        L.pgdg_upload_lists.argtypes = [vp, P(C.c_int64), P(C.c_int64)]
+        L.pgdg_download_lists.argtypes = [vp, P(C.c_int64), P(C.c_int64), P(C.c_int32), C.c_int64, P(C.c_int64)]
+        L.pgdg_download_cell_lists.argtypes = [vp, P(C.c_int64), P(C.c_int64), C.c_int64, P(C.c_int64)]
+        L.pgdg_set_dt.argtypes = [vp, C.c_double]
+        L.pgdg_set_iterate.argtypes = [vp, C.c_int64]
+        L.pgdg_set_max_v.argtypes = [vp, C.c_double]
+        L.pgdg_set_seed_mode.argtypes = [vp, C.c_int]
+        L.pgdg_get_stats.argtypes = [vp, P(pgdg_stats)]
+        L.pgdg_set_timestep.argtypes = [vp, P(C.c_double), P(C.c_double)]
+        L.pgdg_update_grid.argtypes = [vp, C.c_int]
+        L.pgdg_update_particle.argtypes = [vp, C.c_int]
+        L.pgdg_run_step.argtypes = [vp, C.c_int64]
+        L.pgdg_advance.argtypes = [vp, C.c_int]
+        L.pgdg_totals.argtypes = [vp, P(C.c_double)]
+        L.pgdg_mgfm_batched.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                        C.c_int, C.c_void_p, C.c_void_p, C.c_int64]
+        _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# case construction (MPM::Initialize_case restated for the synthetic workloads)
+# ---------------------------------------------------------------------------
+def case_setup(config_id, ncell=None):
+    cs = pgdg_case()
+    nc = (C.c_int32 * 3)(*(ncell or (0, 0, 0)))
+    check(lib().pgdg_case_setup(int(config_id), nc, C.byref(cs)), "pgdg_case_setup")
+    return cs
+
+
+def case_particles(cs, config_id, seed=0):
+    n = lib().pgdg_case_num_particles(C.byref(cs))
+    p = Particles(n, cs.dim)
+    v = p.view()
+    check(lib().pgdg_case_particles(C.byref(cs), int(config_id), int(seed), C.byref(v)), "pgdg_case_particles")
+    return p
+
+
+def case_cells(cs):
+    c = Cells(cs.ncells, cs.dim)
+    check(lib().pgdg_case_cells(C.byref(cs), C.byref(c.view())), "pgdg_case_cells")
+    return c
+
+
+def make_case(config_id, ncell=None, seed=0):
+    cs = case_setup(config_id, ncell)
+    return cs, case_particles(cs, config_id, seed), case_cells(cs)
+
+
+class MPM:
+    """One device context (one case, one GPU)."""
+
+    def __init__(self, cs: pgdg_case, precision=PREC_FP64, capacity=0):
+        self.cs = cs
+        self.dim = cs.dim
+        self.h = C.c_void_p()
+        rc = lib().pgdg_create(C.byref(cs), int(precision), int(capacity), C.byref(self.h))
+        if rc != 0:
+            raise PgdgError(rc, "pgdg_create")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pgdg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            msg = lib().pgdg_last_error(self.h)
+            raise PgdgError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def sync(self):
+        self._ck(lib().pgdg_synchronize(self.h), "pgdg_synchronize")
+
+    # ---- state exchange ----
+    def upload_particles(self, p: Particles):
+        v = p.view()
+        v.n = p.n
+        self._ck(lib().pgdg_upload_particles(self.h, C.byref(v)), "upload_particles")
+
+    def num_particles(self):
+        n = C.c_int64()
+        self._ck(lib().pgdg_num_particles(self.h, C.byref(n)), "num_particles")
+        return n.value
+
+    def download_particles(self):
+        n = self.num_particles()
+        p = Particles(n, self.dim)
+        v = p.view()
+        self._ck(lib().pgdg_download_particles(self.h, C.byref(v)), "download_particles")
+        return p
+
+    def upload_cells(self, c: Cells):
+        self._ck(lib().pgdg_upload_cells(self.h, C.byref(c.view())), "upload_cells")
+
+    def download_cells(self):
+        c = Cells(self.cs.ncells, self.dim)
+        self._ck(lib().pgdg_download_cells(self.h, C.byref(c.view())), "download_cells")
+        return c
+
+    def upload_lists(self, off, ent):
+        off = np.ascontiguousarray(off, np.int64)
+        ent = np.ascontiguousarray(ent if len(ent) else np.zeros(1, np.int64), np.int64)
+        self._ck(lib().pgdg_upload_lists(self.h, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                         ent.ctypes.data_as(C.POINTER(C.c_int64))), "upload_lists")
+
+    def download_lists(self):
+        n = self.num_particles()
+        tot = C.c_int64()
+        off = np.zeros(n + 1, np.int64)
+        stored = np.zeros(max(n, 1), np.int32)
+        P = C.POINTER
+        self._ck(lib().pgdg_download_lists(self.h, off.ctypes.data_as(P(C.c_int64)), None,
+                                           stored.ctypes.data_as(P(C.c_int32)), 0, C.byref(tot)), "download_lists")
+        ent = np.zeros(max(tot.value, 1), np.int64)
+        self._ck(lib().pgdg_download_lists(self.h, off.ctypes.data_as(P(C.c_int64)), ent.ctypes.data_as(P(C.c_int64)),
+                                           stored.ctypes.data_as(P(C.c_int32)), ent.size, C.byref(tot)),
+                 "download_lists")
+        return off, ent[: tot.value], stored[:n]
+
+    def download_cell_lists(self):
+        tot = C.c_int64()
+        off = np.zeros(self.cs.ncells + 1, np.int64)
+        P = C.POINTER
+        self._ck(lib().pgdg_download_cell_lists(self.h, off.ctypes.data_as(P(C.c_int64)), None, 0, C.byref(tot)),
+                 "download_cell_lists")
+        ent = np.zeros(max(tot.value, 1), np.int64)
+        self._ck(lib().pgdg_download_cell_lists(self.h, off.ctypes.data_as(P(C.c_int64)),
+                                                ent.ctypes.data_as(P(C.c_int64)), ent.size, C.byref(tot)),
+                 "download_cell_lists")
+        return off, ent[: tot.value]
+
+    def set_dt(self, dt):
+        self._ck(lib().pgdg_set_dt(self.h, float(dt)), "set_dt")
+
+    def set_iterate(self, n):
+        lib().pgdg_set_iterate(self.h, int(n))
+
+    def set_max_v(self, mv):
+        self._ck(lib().pgdg_set_max_v(self.h, float(mv)), "set_max_v")
+
+    def set_seed_mode(self, mode):
+        self._ck(lib().pgdg_set_seed_mode(self.h, int(mode)), "set_seed_mode")
+
+    def stats(self):
+        s = pgdg_stats()
+        self._ck(lib().pgdg_get_stats(self.h, C.byref(s)), "stats")
+        return s.to_dict()
+
+    def totals(self):
+        out = np.zeros(6)
+        self._ck(lib().pgdg_totals(self.h, out.ctypes.data_as(C.POINTER(C.c_double))), "totals")
+        return out
+
+    # ---- reference methods ----
+    def Set_timestep(self):
+        dt, mv = C.c_double(), C.c_double()
+        self._ck(lib().pgdg_set_timestep(self.h, C.byref(dt), C.byref(mv)), "Set_timestep")
+        return dt.value, mv.value
+
+    def Used_state_update(self):
+        self._ck(lib().pgdg_used_state_update(self.h), "Used_state_update")
+
+    def Map_the_particle_to_tree(self):
+        self._ck(lib().pgdg_bin_particles(self.h), "Map_the_particle_to_tree")
+
+    def Split_particle_fast(self):
+        self._ck(lib().pgdg_split_particle_fast(self.h), "Split_particle_fast")
+
+    def Merge_particle_fast(self):
+        self._ck(lib().pgdg_merge_particle_fast(self.h), "Merge_particle_fast")
+
+    def Refresh_membership(self):
+        self._ck(lib().pgdg_refresh_membership(self.h), "Refresh_membership")
+
+    def Refresh_neighbors(self):
+        self._ck(lib().pgdg_refresh_neighbors(self.h), "Refresh_neighbors")
+
+    def MLS_P2G(self):
+        self._ck(lib().pgdg_mls_p2g(self.h), "MLS_P2G")
+
+    def Calculate_limiter(self):
+        self._ck(lib().pgdg_calculate_limiter(self.h), "Calculate_limiter")
+
+    def Grid_acceleration(self):
+        self._ck(lib().pgdg_grid_acceleration(self.h), "Grid_acceleration")
+
+    def Update_grid(self, md):
+        self._ck(lib().pgdg_update_grid(self.h, int(md)), "Update_grid")
+
+    def Update_particle(self, md):
+        self._ck(lib().pgdg_update_particle(self.h, int(md)), "Update_particle")
+
+    def MPM_run_simulation(self, n):
+        self._ck(lib().pgdg_run_step(self.h, int(n)), "MPM_run_simulation")
+
+    def advance(self, nsteps):
+        self._ck(lib().pgdg_advance(self.h, int(nsteps)), "advance")

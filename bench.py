@@ -1,0 +1,319 @@
+"""Benchmark of the PGDG per-time-step particle-grid path on GB300.
+
+Metric: cell-stage updates/s = (active cells x 2 RK stages x steps) / time of the
+whole step (split, 4x merge, binning, P2G, limiter, DG residual with MGFM,
+update, G2P with particle shifting, CFL reduction).  Workload: the 3D Air/He
+spherical shock-bubble, 384x96x96 cells, 8 particles per cell (28.3 M
+particles), synthetic initial state (seeded lattice), mixed precision.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs N independent replicas (one per GPU, launched by torch.distributed.run);
+the path has no exchange between GPUs.  --impl reference times the CPU
+restatement of the reference's path on the host cores (the reference itself
+cannot be built: it needs Eigen, oneTBB, Boost.MPI and MPI, none of which are
+installed).  One JSON line is printed by rank 0.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "cell-stage updates/s (learned+mixed path, 3D spherical shock-bubble)"
+UNIT = "cell-stage/s"
+WORKLOAD = "3D Air/He spherical shock-bubble, 384x96x96 P1 DG cells, 8 particles/cell"
+CONFIG_ID = 3
+GRID = (384, 96, 96)
+SAMPLE_GRID = (96, 24, 24)      # bounded CPU sample of the same case
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """Sample nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_baseline(steps=1, warmup=1, threads=None):
+    """The CPU restatement (oracle) timed on a bounded sample of the same case."""
+    from oracle import oracle as O
+    from pgdg_p2_gb300 import mpm as M
+    threads = threads or os.cpu_count()
+    O.set_threads(threads)
+    cs, p, c = M.make_case(CONFIG_ID, SAMPLE_GRID)
+    o = O.Oracle(cs)
+    o.upload_particles(p)
+    o.upload_cells(c)
+    o.advance(warmup)
+    t0 = time.perf_counter()
+    o.advance(steps)
+    dt = time.perf_counter() - t0
+    ncell = cs.ncells
+    return {"value": ncell * 2 * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"same case on {SAMPLE_GRID[0]}x{SAMPLE_GRID[1]}x{SAMPLE_GRID[2]} cells "
+                      f"({p.n} particles), {steps} step(s) after {warmup} warm-up, FP64 CPU oracle "
+                      f"(OpenMP, {threads} threads); reference build unavailable (Eigen/oneTBB/Boost.MPI/MPI absent)",
+            "seconds": dt}
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    cb = cpu_baseline(steps=max(1, args.steps // 5), warmup=max(1, min(args.warmup, 2)))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": max(1, args.steps // 5), "warmup": max(1, min(args.warmup, 2)),
+            "ms_per_step": 1e3 * cb["seconds"] / max(1, args.steps // 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_grid": list(SAMPLE_GRID)},
+            "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"]},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def state_bytes(p, c):
+    tot = 0
+    for a in p.as_dict().values():
+        tot += a.nbytes
+    for a in c.as_dict().values():
+        tot += a.nbytes
+    return tot
+
+
+def run_ours(args):
+    ws, rank, local = _dist()
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import ctypes
+    from pgdg_p2_gb300 import mpm as M
+    from pgdg_p2_gb300.abi import PREC_FP64_FMA, PREC_MIXED
+    if ws > 1:
+        # one replica per GPU: select this rank's device before the context exists
+        cudart = ctypes.CDLL("libcudart.so")
+        cudart.cudaSetDevice(local)
+
+    cs, p, c = M.make_case(CONFIG_ID, GRID)
+    ncell = cs.ncells
+    g = M.MPM(cs, PREC_MIXED)
+    g.upload_particles(p)
+    g.upload_cells(c)
+    g.advance(args.warmup)
+    g.sync()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- timed region: K steps, CUDA events on the context stream ----
+    barrier()
+    n0 = g.launch_count()
+    g.profile(True)
+    with Clocks(local) as clk:
+        ms = g.time_advance(args.steps)
+    prof = g.profile_read()
+    g.profile(False)
+    launches = g.launch_count() - n0
+    barrier()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    st = g.stats()
+    value = ws * ncell * 2 * args.steps / (ms / 1e3)
+
+    if args.only_timed:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms / args.steps,
+                              "gpu_launches": launches, "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
+                              "note": "timed region only"}), flush=True)
+        g.close()
+        return
+
+    # ---- end to end through the C ABI with host buffers ----
+    g2 = M.MPM(cs, PREC_MIXED)
+    ke = args.steps
+    nbytes = state_bytes(p, c)
+    t0 = time.perf_counter()
+    g2.upload_particles(p)
+    g2.upload_cells(c)
+    for _ in range(ke):
+        g2.advance(1)
+        g2.stats()                 # device->host read of dt / max_v / counters
+    q = g2.download_particles()
+    cq = g2.download_cells()
+    g2.sync()
+    te = time.perf_counter() - t0
+    dbytes = state_bytes(q, cq)
+    e2e = {"value": ws * ncell * 2 * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes // ke,
+           "d2h_bytes_per_step": dbytes // ke + 160, "steps": ke, "seconds": te}
+    g2.close()
+
+    # ---- plain FP64 GPU path (FMA) on the same case, for the mixed/FP64 ratio ----
+    f = M.MPM(cs, PREC_FP64_FMA)
+    f.upload_particles(p)
+    f.upload_cells(c)
+    f.advance(1)
+    kf = max(1, min(2, args.steps))
+    msf = f.time_advance(kf)
+    fp64 = {"value": ncell * 2 * kf / (msf / 1e3), "ms_per_step": msf / kf, "steps": kf,
+            "speedup_mixed_over_fp64": (ms / args.steps) and (msf / kf) / (ms / args.steps)}
+    # matched-error evidence: both paths after the same number of steps from the same state
+    nsteps_done = args.warmup + args.steps
+    f.advance(nsteps_done - 1 - kf) if nsteps_done - 1 - kf > 0 else None
+    import numpy as np
+    cg, cf = g.download_cells(), f.download_cells()
+    l1 = []
+    for u in range(cs.dim + 2):
+        qg = (cg.alph * cg.coef[:, :, u, 0]).sum(1)
+        qf = (cf.alph * cf.coef[:, :, u, 0]).sum(1)
+        l1.append(float(np.abs(qg - qf).sum() / max(np.abs(qf).sum(), 1e-300)))
+    mom = sum(float(np.abs((cf.alph * cf.coef[:, :, 1 + k, 0]).sum(1)).sum()) for k in range(cs.dim))
+    l1m = [float(np.abs((cg.alph * cg.coef[:, :, 1 + k, 0]).sum(1) - (cf.alph * cf.coef[:, :, 1 + k, 0]).sum(1)).sum()
+                 / max(mom, 1e-300)) for k in range(cs.dim)]
+    fp64["l1_mixed_vs_fp64"] = {"per_variable": l1, "momentum_over_|rho u|": l1m, "steps": nsteps_done}
+    f.close()
+
+    # ---- roofline of the dominant kernel ----
+    import math
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    dom = max((k for k in prof if k not in ("split", "merge")), key=lambda k: prof[k][0]) if prof else None
+    roof = None
+    if dom:
+        d_ms, d_cnt = prof[dom]
+        per_launch_ms = d_ms / d_cnt
+        N = st["n_particles"]
+        # algorithmic bytes per launch (FP32 storage) of the dominant kernel
+        bytes_per = {"pst": N * (2 * 3 * 4 + 2 * 4 + 4 * 4 + 1 + 1 + 3 * 4 + 3 * 4),
+                     "grid_acc": ncell * (2 * 20 * 4 + 2 * 5 * 4 + 2 * 4 + 2 * 20 * 4),
+                     "g2p": N * (3 * 4 * 3 + 4 * 9 + 15 * 4 + 3 * 4 * 2) + ncell * 25 * 4,
+                     "p2g": ncell * (2 * 4 + 2 * 20 * 4) + N * (3 * 4 + 4 + 1),
+                     "limiter": ncell * (2 * 20 * 4 * 1 + 2 * 9 * 4 * 2 + 2 * 5 * 4 + 9 * 4)}.get(dom, 0)
+        achieved = bytes_per / (per_launch_ms / 1e3) / 1e9
+        # FP32 work of the shifting kernel: ~137 pairs x 50 flop per particle (3D, 8 ppc)
+        flops_per = {"pst": N * 137 * 50, "grid_acc": ncell * 13000}.get(dom, 0)
+        sm_mhz = peaks.get("sm_max_mhz", 2070.0)
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "peak_source": "measured" if peaks else "fallback",
+                "per_launch_ms": per_launch_ms, "launches": d_cnt,
+                "fp32": {"achieved_tflops": flops_per / (per_launch_ms / 1e3) / 1e12,
+                         "nominal_peak_tflops": fp32_peak,
+                         "frac": flops_per / (per_launch_ms / 1e3) / 1e12 / fp32_peak}}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cb = cpu_baseline(steps=1, warmup=1)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "cells": ncell, "particles": st["n_particles"],
+                           "precision": "mixed: FP32 DG residual/limiter/G2P/shifting, FP64 MGFM Newton and P2G "
+                                        "moment sums", "mgfm_seed": "plain",
+                           "l2": "inputs larger than L2 (state of several GB streamed every step)",
+                           "parallelism": f"replicas x{ws}"},
+                "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
+                "cpu_baseline": cpu, "fp64_path": fp64,
+                "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
+                "stats": {k: st[k] for k in ("n_particles", "n_split", "n_merge", "n_inlet", "n_outlet",
+                                             "mgfm_calls", "mgfm_iters", "g2p_fallbacks", "list_entries")}}
+        print(json.dumps(line), flush=True)
+    g.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-timed", action="store_true", help="timed region only (profiling runs)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -98,6 +98,17 @@ int pgdg_mgfm_batched(pgdg_ctx* ctx, const double* in6, const int8_t* mat2, cons
                       const double* pinf, int nmat, int variant, int seed_mode, double* out3,
                       int32_t* iters, int64_t n);
 
+/* ---- measurement ----
+ * pgdg_profile: record CUDA events on the context stream around every method
+ * call; pgdg_profile_read returns per-method totals (names ';'-separated, in
+ * first-seen order), pgdg_launch_count the number of kernels launched so far,
+ * pgdg_time_advance the device time of nsteps steps (events on the context
+ * stream, synchronised on both sides). */
+int pgdg_profile(pgdg_ctx* ctx, int enable);
+int pgdg_profile_read(pgdg_ctx* ctx, char* names, int names_cap, double* ms, int64_t* counts, int cap, int* n);
+int pgdg_launch_count(pgdg_ctx* ctx, int64_t* n);
+int pgdg_time_advance(pgdg_ctx* ctx, int nsteps, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

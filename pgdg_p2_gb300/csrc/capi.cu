@@ -57,6 +57,57 @@ struct pgdg_ctx {
   virtual int advance(int) = 0;
   virtual int totals(double*) = 0;
   virtual int check() = 0;
+  /* per-method device timing with CUDA events on the context stream */
+  bool prof = false;
+  int64_t launches = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_next = 0;
+  std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<std::string> knames;
+  std::vector<double> kms;
+  std::vector<int64_t> kcnt;
+  cudaEvent_t ev_get() {
+    if (ev_next >= ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_next++];
+  }
+  void flush_prof() {
+    if (pending.empty()) return;
+    cudaStreamSynchronize(st);
+    for (auto& p : pending) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+      size_t k = 0;
+      for (; k < knames.size(); k++)
+        if (knames[k] == p.first) break;
+      if (k == knames.size()) {
+        knames.push_back(p.first);
+        kms.push_back(0);
+        kcnt.push_back(0);
+      }
+      kms[k] += ms;
+      kcnt[k] += 1;
+    }
+    pending.clear();
+    ev_next = 0;
+  }
+  template <typename Fn>
+  void timed(const char* name, int nlaunch, Fn fn) {
+    launches += nlaunch;
+    if (!prof) {
+      fn();
+      return;
+    }
+    if (ev_next + 2 > 4096) flush_prof();
+    cudaEvent_t a = ev_get(), b = ev_get();
+    cudaEventRecord(a, st);
+    fn();
+    cudaEventRecord(b, st);
+    pending.push_back({name, {a, b}});
+  }
 };
 
 namespace {
@@ -96,6 +147,7 @@ struct Ctx : pgdg_ctx {
 
   ~Ctx() override {
     if (st) cudaStreamSynchronize(st);
+    for (auto e : ev_pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     if (st) cudaStreamDestroy(st);
   }
@@ -535,8 +587,15 @@ struct Ctx : pgdg_ctx {
       len[s] = (int32_t)((int64_t)arena.size() - lo[s]);
     }
     if ((int64_t)arena.size() > K.arena_cap) {
-      err = "list arena too small";
-      return PGDG_EOVERFLOW;
+      /* grow the list arena to hold the uploaded lists */
+      int32_t* na = nullptr;
+      CK(cudaStreamSynchronize(st));
+      CK(dalloc(&na, arena.size() + (size_t)K.cap));
+      for (auto& a : allocs)
+        if (a == (void*)P.arena) a = na;
+      cudaFree(P.arena);
+      P.arena = na;
+      K.arena_cap = (int64_t)arena.size() + K.cap;
     }
     CK(cudaStreamSynchronize(st));
     if (!arena.empty()) CK(cudaMemcpy(P.arena, arena.data(), 4 * arena.size(), cudaMemcpyHostToDevice));
@@ -651,7 +710,7 @@ struct Ctx : pgdg_ctx {
 
   /* ---------------- methods ---------------- */
   int set_timestep(double* dt, double* mv) override {
-    Launch<D, R, EX>::set_timestep(K, P, iterate > 1 ? 1 : 0, st);
+    timed("set_timestep", 3, [&] { Launch<D, R, EX>::set_timestep(K, P, iterate > 1 ? 1 : 0, st); });
     if (dt || mv) {
       DevCounters h = counters();
       if (dt) *dt = h.dt;
@@ -660,19 +719,19 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
   int used_state() override {
-    Launch<D, R, EX>::used_state(K, P, st);
+    timed("used_state", 1, [&] { Launch<D, R, EX>::used_state(K, P, st); });
     return PGDG_OK;
   }
   int bin() override {
-    Launch<D, R, EX>::bin(K, P, st);
+    timed("bin", 2, [&] { Launch<D, R, EX>::bin(K, P, st); });
     return PGDG_OK;
   }
   int split() override {
-    Launch<D, R, EX>::split(K, P, st);
+    timed("split", 12, [&] { Launch<D, R, EX>::split(K, P, st); });
     return PGDG_OK;
   }
   int merge() override {
-    Launch<D, R, EX>::merge(K, P, st);
+    timed("merge", 13, [&] { Launch<D, R, EX>::merge(K, P, st); });
     return PGDG_OK;
   }
   /* flag 4: a cell's particle list is its bucket and a particle's in_ele[0]
@@ -682,19 +741,19 @@ struct Ctx : pgdg_ctx {
    * the shifting kernel; nothing to do here */
   int refresh_neighbors() override { return PGDG_OK; }
   int p2g() override {
-    Launch<D, R, EX>::p2g(K, P, st);
+    timed("p2g", 1, [&] { Launch<D, R, EX>::p2g(K, P, st); });
     return PGDG_OK;
   }
   int limiter() override {
-    Launch<D, R, EX>::limiter(K, P, st);
+    timed("limiter", 1, [&] { Launch<D, R, EX>::limiter(K, P, st); });
     return PGDG_OK;
   }
   int grid_acc() override {
-    Launch<D, R, EX>::grid_acc(K, P, st);
+    timed("grid_acc", 1, [&] { Launch<D, R, EX>::grid_acc(K, P, st); });
     return PGDG_OK;
   }
   int update_grid(int md) override {
-    Launch<D, R, EX>::update_grid(K, P, md, st);
+    timed("update_grid", 1, [&] { Launch<D, R, EX>::update_grid(K, P, md, st); });
     return PGDG_OK;
   }
   int update_particle(int md) override {
@@ -709,9 +768,9 @@ struct Ctx : pgdg_ctx {
       xn = 3 - xs - x0b;
       if (xn == xs || xn == x0 || xn < 0 || xn > 2) xn = (xs + 1) % 3;  /* md 1 without md 0 */
     }
-    Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, st);
-    Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, st);
-    if (md == 1) Launch<D, R, EX>::store_lists(K, P, xs, hs, xn, st);
+    timed("g2p", 1, [&] { Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, st); });
+    timed("pst", 1, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, st); });
+    if (md == 1) timed("store_lists", 2, [&] { Launch<D, R, EX>::store_lists(K, P, xs, hs, xn, st); });
     P.xb = xn;
     P.hb = hn;
     return PGDG_OK;
@@ -830,5 +889,56 @@ int pgdg_update_particle(pgdg_ctx* ctx, int md) { return ctx->update_particle(md
 int pgdg_run_step(pgdg_ctx* ctx, int64_t n) { return ctx->run_step(n); }
 int pgdg_advance(pgdg_ctx* ctx, int nsteps) { return ctx->advance(nsteps); }
 int pgdg_totals(pgdg_ctx* ctx, double* out6) { return ctx->totals(out6); }
+
+int pgdg_profile(pgdg_ctx* ctx, int enable) {
+  ctx->flush_prof();
+  ctx->prof = enable != 0;
+  if (enable) {
+    ctx->knames.clear();
+    ctx->kms.clear();
+    ctx->kcnt.clear();
+  }
+  return PGDG_OK;
+}
+int pgdg_profile_read(pgdg_ctx* ctx, char* names, int names_cap, double* ms, int64_t* counts, int cap, int* n) {
+  ctx->flush_prof();
+  int k = (int)ctx->knames.size();
+  *n = k;
+  std::string all;
+  for (int i = 0; i < k; i++) {
+    if (i < cap) {
+      if (ms) ms[i] = ctx->kms[i];
+      if (counts) counts[i] = ctx->kcnt[i];
+    }
+    all += ctx->knames[i];
+    all += ';';
+  }
+  if (names && names_cap > 0) {
+    std::strncpy(names, all.c_str(), names_cap - 1);
+    names[names_cap - 1] = 0;
+  }
+  return PGDG_OK;
+}
+int pgdg_launch_count(pgdg_ctx* ctx, int64_t* n) {
+  *n = ctx->launches;
+  return PGDG_OK;
+}
+int pgdg_time_advance(pgdg_ctx* ctx, int nsteps, double* ms) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaStreamSynchronize(ctx->st);
+  cudaEventRecord(a, ctx->st);
+  int rc = ctx->advance(nsteps);
+  cudaEventRecord(b, ctx->st);
+  cudaEventSynchronize(b);
+  float f = 0;
+  cudaEventElapsedTime(&f, a, b);
+  *ms = f;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  return ctx->check();
+}
 
 }  // extern "C"

@@ -59,6 +59,10 @@ def lib():
         L.pgdg_run_step.argtypes = [vp, C.c_int64]
         L.pgdg_advance.argtypes = [vp, C.c_int]
         L.pgdg_totals.argtypes = [vp, P(C.c_double)]
+        L.pgdg_profile.argtypes = [vp, C.c_int]
+        L.pgdg_profile_read.argtypes = [vp, C.c_char_p, C.c_int, P(C.c_double), P(C.c_int64), C.c_int, P(C.c_int)]
+        L.pgdg_launch_count.argtypes = [vp, P(C.c_int64)]
+        L.pgdg_time_advance.argtypes = [vp, C.c_int, P(C.c_double)]
         L.pgdg_mgfm_batched.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                         C.c_int, C.c_void_p, C.c_void_p, C.c_int64]
         _lib = L
@@ -248,3 +252,27 @@ class MPM:
 
     def advance(self, nsteps):
         self._ck(lib().pgdg_advance(self.h, int(nsteps)), "advance")
+
+    # ---- measurement ----
+    def time_advance(self, nsteps):
+        """Device time (ms) of nsteps steps, CUDA events on the context stream."""
+        ms = C.c_double()
+        self._ck(lib().pgdg_time_advance(self.h, int(nsteps), C.byref(ms)), "time_advance")
+        return ms.value
+
+    def profile(self, enable=True):
+        self._ck(lib().pgdg_profile(self.h, 1 if enable else 0), "profile")
+
+    def profile_read(self):
+        names = C.create_string_buffer(4096)
+        ms = (C.c_double * 64)()
+        cnt = (C.c_int64 * 64)()
+        n = C.c_int()
+        self._ck(lib().pgdg_profile_read(self.h, names, 4096, ms, cnt, 64, C.byref(n)), "profile_read")
+        keys = names.value.decode().split(";")[: n.value]
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(keys)}
+
+    def launch_count(self):
+        n = C.c_int64()
+        self._ck(lib().pgdg_launch_count(self.h, C.byref(n)), "launch_count")
+        return n.value

@@ -1,0 +1,42 @@
+"""Mixed-precision path (FP32 residual / limiter / G2P / shifting, FP64 MGFM and
+P2G sums) against the FP64 oracle: relative L1 per conserved variable."""
+import numpy as np
+import pytest
+
+from tests.gpu_helpers import conserved_l1
+
+pytestmark = pytest.mark.gpu
+
+# tolerance of the accuracy gate: 1e-3 relative L1 per conserved variable
+# (momentum components normalised by the momentum magnitude, because the
+# transverse components are near zero in most of the domain)
+TOL = 1e-3
+
+
+@pytest.mark.parametrize("cid,grid,steps", [(3, (96, 24, 24), 10), (2, (64, 16, 16), 10), (1, (112, 48), 20),
+                                            (4, (128, 128), 10)])
+def test_mixed_l1_vs_oracle(gpu_mod, oracle_mod, cid, grid, steps):
+    M, O = gpu_mod, oracle_mod
+    from pgdg_p2_gb300.abi import PREC_MIXED
+    cs, p, c = M.make_case(cid, grid)
+    g = M.MPM(cs, PREC_MIXED)
+    o = O.Oracle(cs)
+    for x in (g, o):
+        x.upload_particles(p)
+        x.upload_cells(c)
+    for s in range(1, steps + 1):
+        dt, mv = o.Set_timestep()
+        g.Set_timestep()
+        g.set_dt(dt)
+        g.set_max_v(mv)
+        g.set_iterate(s)
+        o.set_iterate(s)
+        g.MPM_run_simulation(s)
+        o.MPM_run_simulation(s)
+    g.sync()
+    per, mom = conserved_l1(cs, g.download_cells(), o.download_cells())
+    assert per[0] <= TOL, per
+    assert per[-1] <= TOL, per
+    assert max(mom) <= TOL, (per, mom)
+    pg, po = g.download_particles(), o.download_particles()
+    assert abs(pg.n - po.n) <= max(2, po.n // 1000)

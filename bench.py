@@ -156,7 +156,8 @@ def run_ours(args):
         cudart = ctypes.CDLL("libcudart.so")
         cudart.cudaSetDevice(local)
 
-    cs, p, c = M.make_case(CONFIG_ID, GRID)
+    grid = tuple(int(x) for x in args.grid.split(",")) if args.grid else GRID
+    cs, p, c = M.make_case(CONFIG_ID, grid)
     ncell = cs.ncells
     g = M.MPM(cs, PREC_MIXED)
     g.upload_particles(p)
@@ -306,6 +307,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-timed", action="store_true", help="timed region only (profiling runs)")
+    ap.add_argument("--grid", default="", help="override the grid, e.g. 192,48,48 (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -198,6 +198,7 @@ struct Ctx : pgdg_ctx {
     CK(A(&P.c, n)); CK(A(&P.P, n));
     CK(A(&P.rhov, D * n)); CK(A(&P.v, D * n)); CK(A(&P.tv, D * n));
     CK(A(&P.sl, NS * n));
+    CK(A(&P.rec, 8 * n));
     CK(A(&P.phase, n)); CK(A(&P.mark_in, n)); CK(A(&P.seq, n));
     CK(A(&P.lcell, n)); CK(A(&P.lkey, n)); CK(A(&P.list_len, n)); CK(A(&P.list_off, n));
     CK(A(&P.target, n)); CK(A(&P.aff, n)); CK(A(&P.mflag, n)); CK(A(&P.evcode, n));
@@ -586,16 +587,17 @@ struct Ctx : pgdg_ctx {
       }
       len[s] = (int32_t)((int64_t)arena.size() - lo[s]);
     }
-    if ((int64_t)arena.size() > K.arena_cap) {
-      /* grow the list arena to hold the uploaded lists */
+    if ((int64_t)arena.size() + 16 * K.cap > K.arena_cap) {
+      /* grow the list arena to hold the uploaded lists and the ones split/merge add */
       int32_t* na = nullptr;
       CK(cudaStreamSynchronize(st));
-      CK(dalloc(&na, arena.size() + (size_t)K.cap));
+      const size_t ncap = arena.size() * 2 + (size_t)K.cap * 32;
+      CK(dalloc(&na, ncap));
       for (auto& a : allocs)
         if (a == (void*)P.arena) a = na;
       cudaFree(P.arena);
       P.arena = na;
-      K.arena_cap = (int64_t)arena.size() + K.cap;
+      K.arena_cap = (int64_t)ncap;
     }
     CK(cudaStreamSynchronize(st));
     if (!arena.empty()) CK(cudaMemcpy(P.arena, arena.data(), 4 * arena.size(), cudaMemcpyHostToDevice));
@@ -614,10 +616,15 @@ struct Ctx : pgdg_ctx {
     int64_t ns = (int64_t)hc.n_slots;
     std::vector<int32_t> len(std::max<int64_t>(ns, 1));
     std::vector<int64_t> lo(std::max<int64_t>(ns, 1));
-    std::vector<int32_t> arena(std::max<unsigned long long>(hc.arena_used, 1ull));
+    if (hc.err) {
+      err = "device status reports an error; lists are incomplete";
+      return PGDG_ESTATE;
+    }
+    const unsigned long long used = std::min<unsigned long long>(hc.arena_used, (unsigned long long)K.arena_cap);
+    std::vector<int32_t> arena(std::max<unsigned long long>(used, 1ull));
     CK(cudaMemcpy(len.data(), P.list_len, 4 * ns, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(lo.data(), P.list_off, 8 * ns, cudaMemcpyDeviceToHost));
-    if (hc.arena_used) CK(cudaMemcpy(arena.data(), P.arena, 4 * hc.arena_used, cudaMemcpyDeviceToHost));
+    if (used) CK(cudaMemcpy(arena.data(), P.arena, 4 * used, cudaMemcpyDeviceToHost));
     std::vector<int64_t> canon(std::max<int64_t>(ns, 1), -1);
     for (size_t i = 0; i < slots.size(); i++) canon[slots[i]] = (int64_t)i;
     int64_t t = 0;

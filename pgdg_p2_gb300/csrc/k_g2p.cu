@@ -103,6 +103,13 @@ __global__ void __launch_bounds__(128) k_g2p(CaseK K, DevPtrs<R> P, int md, int 
     P.c[p] = c;
     P.mass[p] = vol * rho;
     HN[p] = hroot<D, R>(vol);
+    R* rc = P.rec + 8 * p;
+    for (int d = 0; d < 3; d++) rc[d] = (d < D) ? x[d] : R(0);
+    rc[3] = vol;
+    rc[4] = rho;
+    rc[5] = c;
+    rc[6] = (R)ph;
+    rc[7] = R(0);
   }
   if (nfb) atomicAdd(&P.cnt->g2p_fb, nfb);
 }
@@ -115,98 +122,304 @@ void Launch<D, R, EX>::g2p(const CaseK& K, const DevPtrs<R>& P, int md, int xs, 
 /* ------------------------------------------------------------------ */
 /* particle shifting                                                  */
 /* ------------------------------------------------------------------ */
-template <int D, typename R>
-struct PstAcc {
-  R pst[3], phs[3];
+/* One CTA per brick of cells.  The CTA stages the stage-start position and slot
+ * of every particle in the brick's +-rad2 neighbourhood into shared memory as one
+ * 16-byte (FP32) or 32-byte (FP64) entry, together with per-cell list offsets,
+ * the exact bounding box of each cell's entries and a boundary-particle flag.
+ * Each thread then scans one particle's candidates from shared memory, queues
+ * the members in scan order and sums their contributions in warp-wide batches
+ * (a warp vote flushes every queue together, so the pair arithmetic runs with
+ * full warps).  A particle whose scan range leaves the staged box (it crossed a
+ * cell face during the first stage) reads global memory instead, in the same
+ * order, so both paths give the same result. */
+template <int D>
+struct Brick;
+template <>
+struct Brick<3> {
+  static constexpr int B0 = 4, B1 = 4, B2 = 2;
+};
+template <>
+struct Brick<2> {
+  static constexpr int B0 = 8, B1 = 8, B2 = 1;
+};
+constexpr int PST_THREADS = 256;
+constexpr int PST_BUF = 64;
+
+template <typename R>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  using T = float4;
+};
+template <>
+struct Vec4<double> {
+  using T = double4;
 };
 
+template <int D, typename R>
+struct PstSmem {
+  using V4 = typename Vec4<R>::T;
+  int* off;      /* nsc + 1 */
+  int* mid;      /* nsc: index of the first appended entry of each staged cell */
+  int* bnd;      /* nsc: cell holds boundary particles */
+  R* blo;        /* D * nsc */
+  R* bhi;        /* D * nsc */
+  V4* ent;       /* cap: (x, y, z | slot) of each staged particle at the stage start */
+  unsigned short* buf; /* PST_BUF x PST_THREADS queued member entries */
+  int lo[3], n[3], nsc, cap, maxcnt;
+};
+
+template <int D, typename R>
+__host__ __device__ inline size_t pst_smem_bytes(int nsc, int cap) {
+  size_t b = sizeof(int) * (size_t)(3 * nsc + 1);
+  b = (b + 31) / 32 * 32;
+  b += sizeof(R) * (size_t)(2 * D * nsc);
+  b = (b + 31) / 32 * 32;
+  b += 4 * sizeof(R) * (size_t)cap;
+  b += sizeof(unsigned short) * (size_t)PST_BUF * PST_THREADS;
+  return b + 64;
+}
+
+/* per-particle constants and accumulators of the shifting sum */
 template <int D, typename R, bool EX>
-__global__ void __launch_bounds__(128) k_pst(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn) {
-  const int64_t n = (int64_t)P.cnt->n_slots;
-  const R dt = (R)P.cnt->dt;
-  const R max_v = (R)P.cnt->max_v;
-  const R* XS = P.X[xs];
-  const R* XN = P.X[xn];
-  const R* HS = P.H[hs];
-  const R* HN = P.H[hn];
-  const R cdim = (D == 2) ? R(1.0 / PI_REF) : R(1.0 / PI_REF);
-  GRID_STRIDE(p, n) {
-    const int ph = P.phase[p];
-    if (ph == 0) continue;
-    R xsp[3], xnp[3];
-    for (int d = 0; d < D; d++) {
-      xsp[d] = XS[d * K.cap + p];
-      xnp[d] = XN[d * K.cap + p];
-    }
-    const R hs_p = HS[p], hh = HN[p];
-    const R lim2 = (hs_p * R(CUT_OFF)) * (hs_p * R(CUT_OFF));
-    const R rho_p = P.rho[p], c_p = P.c[p];
+struct PstPart {
+  R xsp[3], xnp[3];
+  R hs_p, hh, lim2, rho_p, c_p, crho_p, tmp1c, C, W_dp, inv_hh, inv_wdp, aw_c;
+  int ph;
+  R pst[3], phs[3];
+
+  __device__ void init(const CaseK& K, R max_v) {
     const R ca = max_v * R(5.);
     const R P_b = rho_p * ca * ca;
     const R hd = (D == 2) ? hh * hh : hh * hh * hh;
-    const R C = (D == 2) ? cdim / hd * R(7. / 4.) : cdim / hd * R(21. / 16.);
+    const R cdim = R(1.0 / PI_REF);
+    C = (D == 2) ? cdim / hd * R(7. / 4.) : cdim / hd * R(21. / 16.);
     const R dxk = hh / R(CELL_RATIO) * R(CUT_OFF);
-    R W_dp;
-    {
-      R s = dxk / hh;
-      R q = R(1.) - R(0.5) * s;
-      W_dp = (s < R(2)) ? C * (((q * q) * q) * q) * (R(1.) + R(2.) * s) : R(0);
+    R s = dxk / hh;
+    R q = R(1.) - R(0.5) * s;
+    W_dp = (s < R(2)) ? C * (((q * q) * q) * q) * (R(1.) + R(2.) * s) : R(0);
+    tmp1c = -R(1.) * P_b * (R(1.) / rho_p);
+    crho_p = c_p * c_p * rho_p;
+    lim2 = (hs_p * R(CUT_OFF)) * (hs_p * R(CUT_OFF));
+    inv_hh = R(1) / hh;
+    inv_wdp = R(1) / W_dp;
+    aw_c = R(-5.) * C * inv_hh * inv_hh; /* dW/dr / r = -5 C q^3 / h^2 */
+    for (int d = 0; d < 3; d++) pst[d] = phs[d] = R(0);
+  }
+
+  __device__ __forceinline__ bool member(const R* xsq) const {
+    R dd = R(0);
+    for (int d = 0; d < D; d++) {
+      R t = xsp[d] - xsq[d];
+      dd = (d == 0) ? t * t : dd + t * t;
     }
-    const R tmp1c = -R(1.) * P_b * (R(1.) / rho_p);
-    const R crho_p = c_p * c_p * rho_p;
-    R pst[3] = {0, 0, 0}, phs[3] = {0, 0, 0};
-    /* scan centre: cell of the stage-start position */
-    int pos[3];
-    cell_pos<D, R>(K, xsp, pos);
-    int lo[3], hi[3];
-    for (int d = 0; d < 3; d++) {
-      int r = (d < D) ? K.rad2 : 0;
-      lo[d] = max(pos[d] - r, 0);
-      hi[d] = min(pos[d] + r, (d < D ? K.N[d] : 1) - 1);
+    if constexpr (EX) return rsqrt_<R>(dd) <= hs_p * R(CUT_OFF); /* get_distance <= h*CUT_OFF */
+    else return dd <= lim2;
+  }
+
+  /* one neighbour's contribution (particle_flow.cpp:540-575) */
+  __device__ __forceinline__ void add(const R* xnq, R volq, R rhoq, R cq, int phq, const R* nq) {
+    R dr[3];
+    R d2 = R(0);
+    for (int d = 0; d < D; d++) {
+      dr[d] = xnp[d] - xnq[d];
+      d2 = (d == 0) ? dr[d] * dr[d] : d2 + dr[d] * dr[d];
     }
-    auto pair = [&](const R* xsq, const R* xnq, R volq, R rhoq, R cq, int phq, const R* nq) {
-      R dd = R(0);
-      for (int d = 0; d < D; d++) {
-        R t = xsp[d] - xsq[d];
-        dd = (d == 0) ? t * t : dd + t * t;
-      }
-      if constexpr (EX) {
-        if (!(rsqrt_<R>(dd) <= hs_p * R(CUT_OFF))) return;  /* get_distance <= h*CUT_OFF */
-      } else {
-        if (!(dd <= lim2)) return;
-      }
-      R dr[3];
-      R d2 = R(0);
-      for (int d = 0; d < D; d++) {
-        dr[d] = xnp[d] - xnq[d];
-        d2 = (d == 0) ? dr[d] * dr[d] : d2 + dr[d] * dr[d];
-      }
+    if (d2 == R(0)) return;
+    R s, q, q3, Wij, aw, rr;
+    if constexpr (EX) {
       R dist = rsqrt_<R>(d2);
-      if (dist == R(0)) return;
-      R s = dist / hh;
-      if (!(s < R(2))) {
-        /* beyond the kernel support: W and dW vanish, but the boundary/interface
-         * terms still see tmp1 = -P_b/rho (contributions are zero) */
-        return;
+      s = dist / hh;
+      if (!(s < R(2))) return; /* W and dW vanish beyond the support */
+      q = R(1.) - R(0.5) * s;
+      q3 = (q * q) * q;
+      Wij = C * (q3 * q) * (R(1.) + R(2.) * s);
+      aw = R(-5.) * C * q3 * s / hh / dist;
+      rr = Wij / W_dp;
+    } else {
+      if constexpr (sizeof(R) == 4) s = d2 * rsqrtf(d2) * inv_hh;
+      else s = rsqrt_<R>(d2) * inv_hh;
+      if (!(s < R(2))) return;
+      q = R(1.) - R(0.5) * s;
+      q3 = (q * q) * q;
+      Wij = C * (q3 * q) * (R(1.) + R(2.) * s);
+      aw = aw_c * q3;
+      rr = Wij * inv_wdp;
+    }
+    R Rr = R(0.2) * ((rr * rr) * (rr * rr));
+    R tmp1 = tmp1c * (R(1) + Rr);
+    if (phq != PGDG_PHASE_BOUNDARY) {
+      for (int d = 0; d < D; d++) pst[d] += dr[d] * aw * tmp1 * volq;
+      if (phq != ph) {
+        R tmp2 = R(1.) / (rho_p + rhoq);
+        R cs = R(-0.1) * tmp2 * (crho_p + cq * cq * rhoq);
+        for (int d = 0; d < D; d++) phs[d] += cs * (dr[d] * aw) * volq;
       }
-      R q = R(1.) - R(0.5) * s;
-      R q3 = (q * q) * q;
-      R Wij = C * (q3 * q) * (R(1.) + R(2.) * s);
-      R aw = R(-5.) * C * q3 * s / hh / dist;
-      R rr = Wij / W_dp;
-      R Rr = R(0.2) * ((rr * rr) * (rr * rr));
-      R tmp1 = tmp1c * (R(1) + Rr);
-      if (phq != PGDG_PHASE_BOUNDARY) {
-        for (int d = 0; d < D; d++) pst[d] += dr[d] * aw * tmp1 * volq;
-        if (phq != ph) {
-          R tmp2 = R(1.) / (rho_p + rhoq);
-          R cs = R(-0.1) * tmp2 * (crho_p + cq * cq * rhoq);
-          for (int d = 0; d < D; d++) phs[d] += cs * (dr[d] * aw) * volq;
-        }
-      } else {
-        for (int d = 0; d < D; d++) pst[d] += nq[d] * Wij * tmp1 * volq;
+    } else {
+      for (int d = 0; d < D; d++) pst[d] += nq[d] * Wij * tmp1 * volq;
+    }
+  }
+};
+
+template <int D, typename R, bool EX>
+__device__ __forceinline__ void pst_boundary_cell(const CaseK& K, const DevPtrs<R>& P, int64_t c,
+                                                  PstPart<D, R, EX>& pp) {
+  for (int e = P.boff[c]; e < P.boff[c + 1]; e++) {
+    int32_t b = P.bent[e];
+    R xb[3], nb[3];
+    for (int d = 0; d < D; d++) {
+      xb[d] = P.bx[d * K.nbnd + b];
+      nb[d] = P.bn[d * K.nbnd + b];
+    }
+    if (pp.member(xb)) pp.add(xb, (R)K.bvol, (R)K.brho, R(0), PGDG_PHASE_BOUNDARY, nb);
+  }
+}
+
+/* member record (new x, vol, rho, c, phase) written by G2P */
+template <int D, typename R, bool EX>
+__device__ __forceinline__ void pst_rec(const DevPtrs<R>& P, int32_t q, PstPart<D, R, EX>& pp) {
+  using V4 = typename Vec4<R>::T;
+  const V4* rc = reinterpret_cast<const V4*>(P.rec + 8 * (int64_t)q);
+  const V4 a = rc[0], b = rc[1];
+  R xnq[3] = {a.x, a.y, a.z};
+  pp.add(xnq, a.w, b.x, b.y, (int)b.z, nullptr);
+}
+
+template <int D, typename R, bool EX>
+__device__ __forceinline__ void pst_fluid(const DevPtrs<R>& P, int32_t q, const R* xsq, PstPart<D, R, EX>& pp) {
+  if (pp.member(xsq)) pst_rec<D, R, EX>(P, q, pp);
+}
+
+template <typename R>
+__device__ __forceinline__ int slot_of(R w);
+template <>
+__device__ __forceinline__ int slot_of<float>(float w) { return __float_as_int(w); }
+template <>
+__device__ __forceinline__ int slot_of<double>(double w) { return (int)w; }
+
+/* one particle: neighbour sum, Bound_pen, Update_PST; sm == nullptr -> global path */
+template <int D, typename R, bool EX>
+__device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, const R* XS, const R* XN, const R* HS,
+                             const R* HN, R dt, R max_v, const PstSmem<D, R>* sm) {
+  PstPart<D, R, EX> pp;
+  pp.ph = P.phase[p];
+  for (int d = 0; d < 3; d++) pp.xsp[d] = pp.xnp[d] = R(0);
+  for (int d = 0; d < D; d++) {
+    pp.xsp[d] = XS[d * K.cap + p];
+    pp.xnp[d] = XN[d * K.cap + p];
+  }
+  pp.hs_p = HS[p];
+  pp.hh = HN[p];
+  pp.rho_p = P.rho[p];
+  pp.c_p = P.c[p];
+  pp.init(K, max_v);
+  /* scan centre: cell of the stage-start position (level_infor.cpp:169-173) */
+  int pos[3];
+  cell_pos<D, R>(K, pp.xsp, pos);
+  int lo[3], hi[3];
+  bool inside = sm != nullptr;
+  for (int d = 0; d < 3; d++) {
+    int r = (d < D) ? K.rad2 : 0;
+    lo[d] = max(pos[d] - r, 0);
+    hi[d] = min(pos[d] + r, (d < D ? K.N[d] : 1) - 1);
+    if (sm && (lo[d] < sm->lo[d] || hi[d] >= sm->lo[d] + sm->n[d])) inside = false;
+  }
+  if (inside) {
+    const R lim2m = pp.lim2 * R(1.0001);
+    int nbuf = 0;
+    /* sum the queued members in queue (= scan) order */
+    auto flush = [&]() {
+      for (int i = 0; i < nbuf; i++) {
+        const int e = sm->buf[i * PST_THREADS + threadIdx.x];
+        pst_rec<D, R, EX>(P, slot_of<R>(sm->ent[e].w), pp);
+      }
+      nbuf = 0;
+    };
+    auto queue = [&](int e) {
+      const auto v = sm->ent[e];
+      R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
+      if (pp.member(xsq)) {
+        if (nbuf == PST_BUF) flush();
+        sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
       }
     };
+    if constexpr (!EX) {
+      /* mixed / FMA paths: each (i, j) row of cells is one contiguous run of
+       * staged entries; trim it to the cells whose bounding box meets the 2h
+       * sphere in z and skip rows whose x/y extent misses it.  Boundary particles
+       * follow in a second pass (the summation order only affects rounding). */
+      const R rr2 = lim2m * rsqrt_<R>(lim2m);
+      const int zl = lo[2] - sm->lo[2], zh = hi[2] - sm->lo[2];
+      for (int t = lo[0]; t <= hi[0]; t++)
+        for (int s = lo[1]; s <= hi[1]; s++) {
+          const int lr = ((t - sm->lo[0]) * sm->n[1] + (s - sm->lo[1])) * sm->n[2];
+          int f = zl, g = zh;
+          if (D == 3) {
+            const R zp = pp.xsp[2];
+            while (f <= g && !(sm->bhi[2 * sm->nsc + lr + f] >= zp - rr2)) f++;
+            while (g >= f && !(sm->blo[2 * sm->nsc + lr + g] <= zp + rr2)) g--;
+          }
+          if (f <= g) {
+            R mx = R(0);
+            for (int d = 0; d < 2; d++) {
+              R a = R(1e30), b = R(-1e30);
+              for (int k = f; k <= g; k++) {
+                a = fmin(a, sm->blo[d * sm->nsc + lr + k]);
+                b = fmax(b, sm->bhi[d * sm->nsc + lr + k]);
+              }
+              R u = a - pp.xsp[d], v = pp.xsp[d] - b;
+              R w = u > v ? u : v;
+              if (w > R(0)) mx += w * w;
+            }
+            if (mx <= lim2m) {
+              const int e0 = sm->off[lr + f], e1 = sm->off[lr + g + 1];
+              for (int e = e0; e < e1; e++) queue(e);
+            }
+          }
+          if (__any_sync(__activemask(), nbuf >= PST_BUF / 2)) flush();
+        }
+      flush();
+      bool edge = false;
+      for (int d = 0; d < D; d++) edge = edge || lo[d] == 0 || hi[d] == K.N[d] - 1;
+      if (edge)
+        for (int t = lo[0]; t <= hi[0]; t++)
+          for (int s = lo[1]; s <= hi[1]; s++)
+            for (int m = lo[2]; m <= hi[2]; m++) {
+              const int l = ((t - sm->lo[0]) * sm->n[1] + (s - sm->lo[1])) * sm->n[2] + (m - sm->lo[2]);
+              if (!sm->bnd[l]) continue;
+              const int64_t c = ((int64_t)t * K.N[1] + s) * K.N[2] + m;
+              pst_boundary_cell<D, R, EX>(K, P, c, pp);
+            }
+    } else {
+      /* exact path: the reference's per-cell list order (binned fluid,
+       * boundary particles, appended fluid) */
+      for (int t = lo[0]; t <= hi[0]; t++)
+        for (int s = lo[1]; s <= hi[1]; s++) {
+          int l = ((t - sm->lo[0]) * sm->n[1] + (s - sm->lo[1])) * sm->n[2] + (lo[2] - sm->lo[2]);
+          for (int m = lo[2]; m <= hi[2]; m++, l++) {
+            const int e0 = sm->off[l], e1 = sm->off[l + 1], em = e0 + sm->mid[l];
+            R md = R(0);
+            for (int d = 0; d < D; d++) {
+              R a = sm->blo[d * sm->nsc + l] - pp.xsp[d];
+              R b = pp.xsp[d] - sm->bhi[d * sm->nsc + l];
+              R g = a > b ? a : b;
+              if (g > R(0)) md += g * g;
+            }
+            if (md <= lim2m)
+              for (int e = e0; e < em; e++) queue(e);
+            if (sm->bnd[l]) {
+              flush();
+              const int64_t c = ((int64_t)t * K.N[1] + s) * K.N[2] + m;
+              pst_boundary_cell<D, R, EX>(K, P, c, pp);
+            }
+            if (md <= lim2m)
+              for (int e = em; e < e1; e++) queue(e);
+            if (__any_sync(__activemask(), nbuf >= PST_BUF / 2)) flush();
+          }
+        }
+      flush();
+    }
+  } else {
     for (int t = lo[0]; t <= hi[0]; t++)
       for (int s = lo[1]; s <= hi[1]; s++)
         for (int m = lo[2]; m <= hi[2]; m++) {
@@ -214,84 +427,232 @@ __global__ void __launch_bounds__(128) k_pst(CaseK K, DevPtrs<R> P, int xs, int 
           const int cnt = min(P.bcnt[c], K.maxpc);
           const int32_t* bk = P.bucket + c * K.maxpc;
           int r = 0;
-          /* Cell_list order: binned fluid particles, boundary particles, then appended ones */
-          for (int pass = 0; pass < 3; pass++) {
-            if (pass == 1) {
-              for (int e = P.boff[c]; e < P.boff[c + 1]; e++) {
-                int32_t b = P.bent[e];
-                R xb[3], nb[3];
-                for (int d = 0; d < D; d++) {
-                  xb[d] = P.bx[d * K.nbnd + b];
-                  nb[d] = P.bn[d * K.nbnd + b];
-                }
-                pair(xb, xb, (R)K.bvol, (R)K.brho, R(0), PGDG_PHASE_BOUNDARY, nb);
-              }
-              continue;
-            }
-            for (; r < cnt; r++) {
-              int32_t q = bk[r];
-              if (pass == 0 && P.lkey[q] >= KEY_APPEND) break;
-              R xsq[3], xnq[3];
-              for (int d = 0; d < D; d++) {
-                xsq[d] = XS[d * K.cap + q];
-                xnq[d] = XN[d * K.cap + q];
-              }
-              pair(xsq, xnq, P.vol[q], P.rho[q], P.c[q], P.phase[q], nullptr);
-            }
+          for (; r < cnt; r++) {
+            int32_t q = bk[r];
+            if (P.lkey[q] >= KEY_APPEND) break;
+            R xsq[3] = {0, 0, 0};
+            for (int d = 0; d < D; d++) xsq[d] = XS[d * K.cap + q];
+            pst_fluid<D, R, EX>(P, q, xsq, pp);
+          }
+          pst_boundary_cell<D, R, EX>(K, P, c, pp);
+          for (; r < cnt; r++) {
+            int32_t q = bk[r];
+            R xsq[3] = {0, 0, 0};
+            for (int d = 0; d < D; d++) xsq[d] = XS[d * K.cap + q];
+            pst_fluid<D, R, EX>(P, q, xsq, pp);
           }
         }
-    /* Bound_pen (particle_flow.cpp:587-622) on the faces of the particle's cell */
-    R bp[3] = {0, 0, 0};
-    {
-      const int64_t ci = P.lcell[p];
-      int idx[3];
-      idx[2] = (int)(ci % K.N[2]);
-      idx[1] = (int)((ci / K.N[2]) % K.N[1]);
-      idx[0] = (int)(ci / ((int64_t)K.N[1] * K.N[2]));
-      const int fax[6] = {1, 0, 1, 0, 2, 2};
-      const int fsg[6] = {-1, 1, 1, -1, -1, 1};
-      const int fside[6] = {2, 1, 3, 0, 4, 5};
-      for (int f = 0; f < 2 * D; f++) {
-        int a = fax[f];
-        int nbi = idx[a] + fsg[f];
-        if (nbi >= 0 && nbi < K.N[a]) continue;
-        if (K.bc[fside[f]] == 0) continue;
-        R cen = (R)(K.bl[a] + K.ps[a] * (idx[a] + 0.5) + fsg[f] * 0.5 * K.ps[a]);
-        R nn = (R)fsg[f];
-        R ds = (xnp[a] - cen) * nn;
-        if (ds < R(0)) nn = -nn;
-        R dis = fabs(ds);
-        if (dis < R(0.4) * (R)K.p_sz) bp[a] += R(0.02) / dis * (c_p * c_p) * nn;
+  }
+  /* Bound_pen (particle_flow.cpp:587-622) on the faces of the particle's cell */
+  R bp[3] = {0, 0, 0};
+  {
+    const int64_t ci = P.lcell[p];
+    int idx[3];
+    idx[2] = (int)(ci % K.N[2]);
+    idx[1] = (int)((ci / K.N[2]) % K.N[1]);
+    idx[0] = (int)(ci / ((int64_t)K.N[1] * K.N[2]));
+#pragma unroll
+    for (int f = 0; f < 2 * D; f++) {
+      const int a = (f == 0 || f == 2) ? 1 : (f == 1 || f == 3) ? 0 : 2;
+      const int sg = (f == 0 || f == 3 || f == 4) ? -1 : 1;
+      const int side = (f == 0) ? 2 : (f == 1) ? 1 : (f == 2) ? 3 : (f == 3) ? 0 : (f == 4) ? 4 : 5;
+      int nbi = idx[a] + sg;
+      if (nbi >= 0 && nbi < K.N[a]) continue;
+      if (K.bc[side] == 0) continue;
+      R cen = (R)(K.bl[a] + K.ps[a] * (idx[a] + 0.5) + sg * 0.5 * K.ps[a]);
+      R nn = (R)sg;
+      R ds = (pp.xnp[a] - cen) * nn;
+      if (ds < R(0)) nn = -nn;
+      R dis = fabs(ds);
+      if (dis < R(0.4) * (R)K.p_sz) bp[a] += R(0.02) / dis * (pp.c_p * pp.c_p) * nn;
+    }
+  }
+  /* Update_PST (particle_flow.cpp:485-525) */
+  const R px = (R)K.p_sz;
+  R dx[3], dx1[3], dx2[3];
+  R s0 = 0, s1 = 0, s2 = 0;
+  for (int d = 0; d < D; d++) {
+    dx[d] = pp.pst[d] * dt * dt / R(2.);
+    dx1[d] = pp.phs[d] * dt * dt / R(2.);
+    dx2[d] = bp[d] * dt * dt / R(2.);
+    s0 = (d == 0) ? dx[d] * dx[d] : s0 + dx[d] * dx[d];
+    s1 = (d == 0) ? dx1[d] * dx1[d] : s1 + dx1[d] * dx1[d];
+    s2 = (d == 0) ? dx2[d] * dx2[d] : s2 + dx2[d] * dx2[d];
+  }
+  R dis0 = rsqrt_<R>(s0), dis1 = rsqrt_<R>(s1), dis2 = rsqrt_<R>(s2);
+  R l0 = amin1(px / R(10), dis0) / (dis0 + R(1e-20));
+  R l1 = amin1(px / R(10), dis1) / (dis1 + R(1e-20));
+  R l2 = amin1(px / R(2), dis2) / (dis2 + R(1e-20));
+  const bool mk = P.mark_in[p] == 1;
+  for (int d = 0; d < D; d++) {
+    R dv = (dx[d] * l0 + dx1[d] * l1 + dx2[d] * l2) / dt;
+    if (mk) dv = R(0);
+    P.tv[d * K.cap + p] = P.v[d * K.cap + p] + dv;
+  }
+}
+
+template <int D, typename R, bool EX>
+__global__ void __launch_bounds__(PST_THREADS, 2) k_pst(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn,
+                                                    int nb0, int nb1, int cap) {
+  using BK = Brick<D>;
+  using V4 = typename Vec4<R>::T;
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  const R dt = (R)P.cnt->dt;
+  const R max_v = (R)P.cnt->max_v;
+  const R* XS = P.X[xs];
+  const R* XN = P.X[xn];
+  const R* HS = P.H[hs];
+  const R* HN = P.H[hn];
+  const int b = blockIdx.x;
+  int c0[3];
+  /* blockIdx = (i_b * nb1 + j_b) * nb0 + k_b */
+  c0[0] = (b / (nb0 * nb1)) * BK::B0;
+  c0[1] = ((b / nb0) % nb1) * BK::B1;
+  c0[2] = (D == 3) ? (b % nb0) * BK::B2 : 0;
+  const int bdim[3] = {BK::B0, BK::B1, D == 3 ? BK::B2 : 1};
+  PstSmem<D, R> sm;
+  for (int d = 0; d < 3; d++) {
+    int r = (d < D) ? K.rad2 : 0;
+    int Nd = (d < D) ? K.N[d] : 1;
+    int lo = max(c0[d] - r, 0);
+    int hi = min(c0[d] + bdim[d] - 1 + r, Nd - 1);
+    sm.lo[d] = lo;
+    sm.n[d] = hi - lo + 1;
+  }
+  sm.nsc = sm.n[0] * sm.n[1] * sm.n[2];
+  sm.cap = cap;
+  sm.off = reinterpret_cast<int*>(smem_raw);
+  sm.mid = sm.off + sm.nsc + 1;
+  sm.bnd = sm.mid + sm.nsc;
+  size_t o = sizeof(int) * (size_t)(3 * sm.nsc + 1);
+  o = (o + 31) / 32 * 32;
+  sm.blo = reinterpret_cast<R*>(smem_raw + o);
+  sm.bhi = sm.blo + D * sm.nsc;
+  o += sizeof(R) * (size_t)(2 * D * sm.nsc);
+  o = (o + 31) / 32 * 32;
+  sm.ent = reinterpret_cast<V4*>(smem_raw + o);
+  sm.buf = reinterpret_cast<unsigned short*>(sm.ent + cap);
+  __shared__ int s_total, s_maxcnt;
+  for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
+    int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
+    int64_t c = ((int64_t)(sm.lo[0] + t) * K.N[1] + (sm.lo[1] + s)) * K.N[2] + (sm.lo[2] + m);
+    int cnt = min(P.bcnt[c], K.maxpc);
+    sm.off[l + 1] = cnt;
+    sm.mid[l] = cnt;
+    sm.bnd[l] = P.boff[c + 1] > P.boff[c] ? 1 : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int mx = 0;
+    sm.off[0] = 0;
+    for (int l = 0; l < sm.nsc; l++) {
+      mx = max(mx, sm.off[l + 1]);
+      sm.off[l + 1] += sm.off[l];
+    }
+    s_total = sm.off[sm.nsc];
+    s_maxcnt = mx;
+  }
+  __syncthreads();
+  sm.maxcnt = s_maxcnt;
+  const bool use_sm = s_total <= cap;
+  if (use_sm) {
+    for (int e = threadIdx.x; e < s_total; e += blockDim.x) {
+      int lo = 0, hi = sm.nsc - 1;
+      while (lo < hi) {
+        int md = (lo + hi + 1) >> 1;
+        if (sm.off[md] <= e) lo = md;
+        else hi = md - 1;
+      }
+      const int l = lo, r = e - sm.off[l];
+      int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
+      int64_t c = ((int64_t)(sm.lo[0] + t) * K.N[1] + (sm.lo[1] + s)) * K.N[2] + (sm.lo[2] + m);
+      const int32_t* bk = P.bucket + c * K.maxpc;
+      int32_t q = bk[r];
+      V4 v;
+      v.x = XS[q];
+      v.y = XS[K.cap + q];
+      if constexpr (D == 3) {
+        v.z = XS[2 * K.cap + q];
+        if constexpr (sizeof(R) == 4) v.w = __int_as_float(q);
+        else v.w = (R)q;
+      } else {
+        if constexpr (sizeof(R) == 4) v.w = __int_as_float(q);
+        else v.w = (R)q;
+        v.z = R(0);
+      }
+      sm.ent[e] = v;
+      if (P.lkey[q] >= KEY_APPEND && (r == 0 || P.lkey[bk[r - 1]] < KEY_APPEND)) sm.mid[l] = r;
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
+      R mn[3] = {R(1e30), R(1e30), R(1e30)}, mx[3] = {R(-1e30), R(-1e30), R(-1e30)};
+      for (int e = sm.off[l]; e < sm.off[l + 1]; e++) {
+        const V4 v = sm.ent[e];
+        const R xv[3] = {v.x, v.y, v.z};
+        for (int d = 0; d < D; d++) {
+          mn[d] = xv[d] < mn[d] ? xv[d] : mn[d];
+          mx[d] = xv[d] > mx[d] ? xv[d] : mx[d];
+        }
+      }
+      for (int d = 0; d < D; d++) {
+        sm.blo[d * sm.nsc + l] = mn[d];
+        sm.bhi[d * sm.nsc + l] = mx[d];
       }
     }
-    /* Update_PST (particle_flow.cpp:485-525) */
-    const R px = (R)K.p_sz;
-    R dx[3], dx1[3], dx2[3];
-    R s0 = 0, s1 = 0, s2 = 0;
-    for (int d = 0; d < D; d++) {
-      dx[d] = pst[d] * dt * dt / R(2.);
-      dx1[d] = phs[d] * dt * dt / R(2.);
-      dx2[d] = bp[d] * dt * dt / R(2.);
-      s0 = (d == 0) ? dx[d] * dx[d] : s0 + dx[d] * dx[d];
-      s1 = (d == 0) ? dx1[d] * dx1[d] : s1 + dx1[d] * dx1[d];
-      s2 = (d == 0) ? dx2[d] * dx2[d] : s2 + dx2[d] * dx2[d];
+    __syncthreads();
+  }
+  /* the brick's own particles */
+  const int nbc = bdim[0] * bdim[1] * bdim[2];
+  __shared__ int s_boff[BK::B0 * BK::B1 * BK::B2 + 1];
+  __shared__ int s_bcell[BK::B0 * BK::B1 * BK::B2];
+  if (threadIdx.x == 0) {
+    s_boff[0] = 0;
+    for (int q = 0; q < nbc; q++) {
+      int dt0 = q / (bdim[1] * bdim[2]), dt1 = (q / bdim[2]) % bdim[1], dt2 = q % bdim[2];
+      int ci = c0[0] + dt0, cj = c0[1] + dt1, ck = c0[2] + dt2;
+      int cnt = 0;
+      int64_t c = -1;
+      if (ci < K.N[0] && cj < K.N[1] && ck < K.N[2]) {
+        c = ((int64_t)ci * K.N[1] + cj) * K.N[2] + ck;
+        cnt = min(P.bcnt[c], K.maxpc);
+      }
+      s_bcell[q] = (int)c;
+      s_boff[q + 1] = s_boff[q] + cnt;
     }
-    R dis0 = rsqrt_<R>(s0), dis1 = rsqrt_<R>(s1), dis2 = rsqrt_<R>(s2);
-    R l0 = amin1(px / R(10), dis0) / (dis0 + R(1e-20));
-    R l1 = amin1(px / R(10), dis1) / (dis1 + R(1e-20));
-    R l2 = amin1(px / R(2), dis2) / (dis2 + R(1e-20));
-    const bool mk = P.mark_in[p] == 1;
-    for (int d = 0; d < D; d++) {
-      R dv = (dx[d] * l0 + dx1[d] * l1 + dx2[d] * l2) / dt;
-      if (mk) dv = R(0);
-      P.tv[d * K.cap + p] = P.v[d * K.cap + p] + dv;
-    }
+  }
+  __syncthreads();
+  const int npart = s_boff[nbc];
+  for (int i = threadIdx.x; i < npart; i += blockDim.x) {
+    int q = 0;
+    while (s_boff[q + 1] <= i) q++;
+    const int64_t c = s_bcell[q];
+    const int32_t p = P.bucket[c * K.maxpc + (i - s_boff[q])];
+    pst_particle<D, R, EX>(K, P, p, XS, XN, HS, HN, dt, max_v, use_sm ? &sm : nullptr);
   }
 }
 
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, cudaStream_t st) {
-  k_pst<D, R, EX><<<grid_for(K.cap, 128), 128, 0, st>>>(K, P, xs, hs, xn, hn);
+  using BK = Brick<D>;
+  const int nb0 = (D == 3) ? (K.N[2] + BK::B2 - 1) / BK::B2 : 1;
+  const int nb1 = (K.N[1] + BK::B1 - 1) / BK::B1;
+  const int nbx = (K.N[0] + BK::B0 - 1) / BK::B0;
+  const int r = K.rad2;
+  const int nsc = (BK::B0 + 2 * r) * (BK::B1 + 2 * r) * (D == 3 ? BK::B2 + 2 * r : 1);
+  const int ppc = (D == 3) ? 8 : 4;
+  int cap = nsc * ppc * 5 / 4;
+  if (cap > 65535) cap = 65535;
+  size_t bytes = pst_smem_bytes<D, R>(nsc, cap);
+  while (bytes > 220 * 1024 && cap > 256) {
+    cap = cap * 3 / 4;
+    bytes = pst_smem_bytes<D, R>(nsc, cap);
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_pst<D, R, EX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 224 * 1024);
+    attr_set = true;
+  }
+  k_pst<D, R, EX><<<nbx * nb1 * nb0, PST_THREADS, bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap);
 }
 
 #define PGDG_INST(D, R, EX)                                                                              \

@@ -85,6 +85,8 @@ struct DevPtrs {
   R *vol, *vol0, *mass, *rho, *E, *c, *P;
   R *rhov, *v, *tv; /* D*cap */
   R* sl;            /* U*D*cap: coef[0] columns 1..D */
+  R* rec;           /* 8*cap: per-particle record read by the shifting sum
+                     * (new x[3], vol, rho, c, phase, 0), written by G2P */
   int8_t* phase;    /* 0 = tombstone */
   int8_t* mark_in;
   uint64_t* seq;

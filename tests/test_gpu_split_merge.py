@@ -64,6 +64,7 @@ def test_split_merge_bitwise(gpu_mod, oracle_mod, cid, grid, steps, outlet, inle
     o.Map_the_particle_to_tree()
     g.Split_particle_fast()
     o.Split_particle_fast()
+    g.sync()
     assert particles_bitwise_equal(g.download_particles(), o.download_particles()) == []
     gl, ol = g.download_cell_lists(), o.download_cell_lists()
     assert np.array_equal(gl[0], ol[0]) and np.array_equal(gl[1], ol[1])
@@ -77,6 +78,7 @@ def test_split_merge_bitwise(gpu_mod, oracle_mod, cid, grid, steps, outlet, inle
     for it in range(4):
         g.Merge_particle_fast()
         o.Merge_particle_fast()
+        g.sync()
         assert particles_bitwise_equal(g.download_particles(), o.download_particles()) == [], f"merge pass {it}"
         gl, ol = g.download_cell_lists(), o.download_cell_lists()
         assert np.array_equal(gl[0], ol[0]) and np.array_equal(gl[1], ol[1])

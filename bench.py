@@ -26,7 +26,7 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-METRIC = "cell-stage updates/s (learned+mixed path, 3D spherical shock-bubble)"
+METRIC = "cell-stage updates/s, learned+mixed vs plain FP64 on GB300 at matched L1 error"
 UNIT = "cell-stage/s"
 WORKLOAD = "3D Air/He spherical shock-bubble, 384x96x96 P1 DG cells, 8 particles/cell"
 CONFIG_ID = 3
@@ -156,10 +156,17 @@ def run_ours(args):
         cudart = ctypes.CDLL("libcudart.so")
         cudart.cudaSetDevice(local)
 
+    from pgdg_p2_gb300 import surrogate as S
+    params = S.load_default()
+    if params is None:
+        raise SystemExit("trained seed weights missing (python -m pgdg_p2_gb300.train_surrogate)")
+    net = S.Surrogate(params)
+
     grid = tuple(int(x) for x in args.grid.split(",")) if args.grid else GRID
     cs, p, c = M.make_case(CONFIG_ID, grid)
     ncell = cs.ncells
     g = M.MPM(cs, PREC_MIXED)
+    g.set_surrogate(net)
     g.upload_particles(p)
     g.upload_cells(c)
     g.advance(args.warmup)
@@ -199,6 +206,7 @@ def run_ours(args):
 
     # ---- end to end through the C ABI with host buffers ----
     g2 = M.MPM(cs, PREC_MIXED)
+    g2.set_surrogate(net)
     ke = args.steps
     nbytes = state_bytes(p, c)
     t0 = time.perf_counter()
@@ -240,6 +248,19 @@ def run_ours(args):
                  / max(mom, 1e-300)) for k in range(cs.dim)]
     fp64["l1_mixed_vs_fp64"] = {"per_variable": l1, "momentum_over_|rho u|": l1m, "steps": nsteps_done}
     f.close()
+
+    # ---- ablation: mixed path with the reference's inline MGFM and plain seed ----
+    a = M.MPM(cs, PREC_MIXED)
+    a.upload_particles(p)
+    a.upload_cells(c)
+    a.advance(args.warmup)
+    msa = a.time_advance(kf)
+    ablation = {"mixed_inline_plain_seed": {"value": ncell * 2 * kf / (msa / 1e3), "ms_per_step": msa / kf,
+                                            "steps": kf}}
+    a.close()
+
+    # ---- batched MGFM micro-benchmark (2^24 problems), plain vs learned seed ----
+    c5 = None if args.no_c5 else c5_bench(M, S, net)
 
     # ---- roofline of the dominant kernel ----
     import math
@@ -284,19 +305,65 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "cells": ncell, "particles": st["n_particles"],
                            "precision": "mixed: FP32 DG residual/limiter/G2P/shifting, FP64 MGFM Newton and P2G "
-                                        "moment sums", "mgfm_seed": "plain",
+                                        "moment sums", "mgfm_seed": "learned (12-64-64-64-2 MLP, BF16 weights) with plain-Newton fallback; interface problems batched per stage",
                            "l2": "inputs larger than L2 (state of several GB streamed every step)",
                            "parallelism": f"replicas x{ws}"},
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
-                "cpu_baseline": cpu, "fp64_path": fp64,
+                "cpu_baseline": cpu, "fp64_path": fp64, "ablation": ablation, "mgfm_c5": c5,
                 "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
                 "stats": {k: st[k] for k in ("n_particles", "n_split", "n_merge", "n_inlet", "n_outlet",
                                              "mgfm_calls", "mgfm_iters", "g2p_fallbacks", "list_entries")}}
         print(json.dumps(line), flush=True)
     g.close()
+    net.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def c5_bench(M, S, net, n=1 << 24, reps=3):
+    """2^24 seeded two-material problems (splitmix64 seed 5): device time of the
+    batched solve from the plain seed and from the learned seed (inputs resident),
+    mean/max Newton iterations, and the largest relative p* difference among the
+    problems the plain solve converged on."""
+    import numpy as np
+    import torch
+    in6, mat = S.c5_problems(n, seed=5)
+    dev = torch.device("cuda:0")
+    t_in = torch.tensor(in6, device=dev)
+    t_m = torch.tensor(mat, device=dev)
+    t_g = torch.tensor(S.C5_GAMMA, device=dev)
+    t_p = torch.tensor(S.C5_PINF, device=dev)
+    out = {}
+    res = {}
+    L = M.lib()
+    for key, h in (("plain", None), ("learned", net.h)):
+        o = torch.zeros((n, 3), dtype=torch.float64, device=dev)
+        it = torch.zeros(n, dtype=torch.int32, device=dev)
+        args = (h, t_in.data_ptr(), t_m.data_ptr(), t_g.data_ptr(), t_p.data_ptr(), 4, 0, o.data_ptr(),
+                it.data_ptr(), n)
+        for _ in range(2):
+            M.check(L.pgdg_mgfm_batched(*args), "pgdg_mgfm_batched")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.default_stream())
+        for _ in range(reps):
+            M.check(L.pgdg_mgfm_batched(*args), "pgdg_mgfm_batched")
+        e1.record(torch.cuda.default_stream())
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        itn = it.cpu().numpy()
+        res[key] = (o.cpu().numpy(), itn)
+        out[key] = {"problems_per_s": n / (ms / 1e3), "ms": ms, "mean_iters": float(itn.mean()),
+                    "max_iters": int(itn.max())}
+    conv = res["plain"][1] < 50
+    rel = np.abs(res["learned"][0][conv, 1] - res["plain"][0][conv, 1]) / res["plain"][0][conv, 1]
+    out["n"] = n
+    out["with_root"] = float(conv.mean())
+    out["mean_iters_root"] = {k: float(res[k][1][conv].mean()) for k in res}
+    out["max_rel_dp"] = float(rel.max())
+    out["speedup_learned_over_plain"] = out["plain"]["ms"] / out["learned"]["ms"]
+    return out
 
 
 def main():
@@ -306,6 +373,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-c5", action="store_true", help="skip the batched MGFM micro-benchmark")
     ap.add_argument("--only-timed", action="store_true", help="timed region only (profiling runs)")
     ap.add_argument("--grid", default="", help="override the grid, e.g. 192,48,48 (profiling runs)")
     args = ap.parse_args()

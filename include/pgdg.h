@@ -29,8 +29,6 @@ typedef struct pgdg_ctx pgdg_ctx;
  *   FP64_FMA  all FP64 with FMA contraction (the plain FP64 GPU path timed
  *             against MIXED) */
 enum { PGDG_PREC_FP64 = 0, PGDG_PREC_MIXED = 1, PGDG_PREC_FP64_FMA = 2 };
-/* MGFM Newton seed */
-enum { PGDG_SEED_PLAIN = 0, PGDG_SEED_MLP = 1 };
 
 /* ---- case construction (replaces MPM::Initialize_case, mpm_ini.cpp:33-673) ----
  * config_id 1..4 are the synthetic workloads: 1 2D triple point 112x48,
@@ -66,7 +64,6 @@ int pgdg_download_cell_lists(pgdg_ctx* ctx, int64_t* off, int64_t* ent, int64_t 
 int pgdg_set_dt(pgdg_ctx* ctx, double dt);                 /* Solver clip of glbl_timestep (solver.cpp:40-44) */
 int pgdg_set_iterate(pgdg_ctx* ctx, int64_t iterate_num);
 int pgdg_set_max_v(pgdg_ctx* ctx, double max_v);
-int pgdg_set_seed_mode(pgdg_ctx* ctx, int mode);           /* PGDG_SEED_PLAIN / PGDG_SEED_MLP */
 int pgdg_get_stats(pgdg_ctx* ctx, pgdg_stats* st);
 int pgdg_synchronize(pgdg_ctx* ctx);
 
@@ -89,14 +86,47 @@ int pgdg_run_step(pgdg_ctx* ctx, int64_t n);                       /* MPM::MPM_r
 int pgdg_advance(pgdg_ctx* ctx, int nsteps);
 int pgdg_totals(pgdg_ctx* ctx, double* out6);                      /* conservation totals (Triple_point_2phase/mpm_ini.cpp:599-654) */
 
+/* ---- MGFM seed surrogate (new; the reference starts Newton from max(p_l,p_r),
+ *      mpm.cpp:893) ----
+ * A 12-64-64-64-2 tanh MLP predicting the star pressure and velocity of a
+ * two-material Riemann problem; BF16 weights (bf16 = 1) or FP32 weights
+ * (bf16 = 0, for gradient checks), FP32 accumulation.  Parameters are
+ * pgdg_surrogate_num_params() floats: weights, biases and the fixed
+ * feature/target normalisation.  Array arguments are device pointers unless
+ * named *_host. */
+typedef struct pgdg_mlp pgdg_mlp;
+int pgdg_surrogate_create(int bf16, pgdg_mlp** out);
+int pgdg_surrogate_destroy(pgdg_mlp* net);
+int pgdg_surrogate_num_params(void);
+int pgdg_surrogate_set_params(pgdg_mlp* net, const float* params_host);
+int pgdg_surrogate_get_params(pgdg_mlp* net, float* params_host);
+int pgdg_surrogate_features(const double* in6, const int8_t* mat2, const double* gam, const double* pinf, float* X,
+                            int64_t n);
+int pgdg_surrogate_forward(pgdg_mlp* net, const float* X, float* Y, int64_t n);
+int pgdg_surrogate_gradients(pgdg_mlp* net, const float* X, const float* T, int64_t n, float* grad_host,
+                             double* loss);
+int pgdg_surrogate_train_step(pgdg_mlp* net, const float* X, const float* T, int64_t n, float lr, double* loss);
+/* attach a surrogate to a context: the mixed-precision step then seeds every
+ * interface MGFM solve with it (NULL detaches).  Attaching turns the interface
+ * queue on.  Not available on the exact-order FP64 path (PGDG_EINVAL). */
+int pgdg_set_surrogate(pgdg_ctx* ctx, pgdg_mlp* net);
+/* interface queue (no reference counterpart: MPM::Grid_acceleration calls
+ * MGFM inline, particle_flow.cpp:192-204): the residual gathers each stage's
+ * two-material interface problems into one batch, solves them together and
+ * reads the ghost states back.  Mixed and FP64_FMA paths only. */
+int pgdg_set_iface_queue(pgdg_ctx* ctx, int on);
+/* copy the last stage's queued problems to the host (in6 n x 6, mat2 n x 2,
+ * at most cap entries); *n receives the queue length */
+int pgdg_iface_download(pgdg_ctx* ctx, double* in6, int8_t* mat2, int64_t cap, int64_t* n);
+
 /* ---- MGFM interface Riemann solve (mpm.cpp:882-926), batched ----
  * in6: n x (u_l, u_r, p_l, p_r, rho_l, rho_r); mat2: n x (material l, material r)
  * into gam/pinf (nmat entries); out3: n x (rho*_L, p*, u*); iters may be NULL.
- * Pointers are device pointers; stream 0 ordering; seed_mode selects the plain
- * max(p_l,p_r) start or the learned start. */
-int pgdg_mgfm_batched(pgdg_ctx* ctx, const double* in6, const int8_t* mat2, const double* gam,
-                      const double* pinf, int nmat, int variant, int seed_mode, double* out3,
-                      int32_t* iters, int64_t n);
+ * net == NULL starts Newton from the reference's plain seed; otherwise from the
+ * surrogate's prediction, falling back to the plain solve when the seeded one
+ * does not converge.  Device pointers; the default stream. */
+int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2, const double* gam,
+                      const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n);
 
 /* ---- measurement ----
  * pgdg_profile: record CUDA events on the context stream around every method

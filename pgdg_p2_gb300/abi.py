@@ -17,7 +17,6 @@ ERRORS = {
 BC_INTERIOR, BC_WALL, BC_INLET, BC_OUTLET, BC_SYMMETRY, BC_TRANSMISSIVE = 0, 1, -1, -2, -3, -4
 MGFM_3D, MGFM_2D = 0, 1
 PREC_FP64, PREC_MIXED, PREC_FP64_FMA = 0, 1, 2
-SEED_PLAIN, SEED_MLP = 0, 1
 F = 2
 
 

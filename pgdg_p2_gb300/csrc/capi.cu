@@ -26,7 +26,10 @@ struct pgdg_ctx {
   std::string err;
   pgdg_case cs;
   int precision = PGDG_PREC_FP64;
-  int seed_mode = PGDG_SEED_PLAIN;
+  void* net = nullptr;   /* attached seed surrogate (pgdg_mlp) */
+  int iface_queue = 0;   /* 1: interface problems solved as one batch */
+  int64_t iface_last = 0;
+  virtual int iface_download(double*, int8_t*, int64_t, int64_t*) = 0;
   int64_t iterate = 0;
   cudaStream_t st = nullptr;
   virtual int upload_particles(const pgdg_particles*) = 0;
@@ -137,6 +140,9 @@ struct Ctx : pgdg_ctx {
   std::vector<void*> allocs;
   int x0b = 0;          /* step-start coordinate buffer (md 1) */
   double* d_tot = nullptr;
+  IfaceQ Q{};
+  double *d_gam = nullptr, *d_pinf = nullptr;
+  unsigned long long* d_ncell = nullptr;
 
   template <typename T>
   cudaError_t A(T** p, size_t n) {
@@ -217,6 +223,24 @@ struct Ctx : pgdg_ctx {
     P.qcap = (int64_t)nc;
     CK(A(&P.cnt, 1));
     CK(A(&d_tot, 6));
+    /* interface queue: at most 2 phases x 2D faces x 4 points x 1 other phase per cell;
+     * sized for a few per cent of the cells, grown on demand */
+    Q.cap = std::max<int64_t>(1 << 16, K.ncell / 8);
+    CK(A(&Q.in6, 6 * (size_t)Q.cap));
+    CK(A(&Q.mat, 2 * (size_t)Q.cap));
+    CK(A(&Q.out3, 3 * (size_t)Q.cap));
+    CK(A(&Q.off, nc + 1));
+    CK(A(&Q.blk, (nc + 2047) / 2048 + 2));
+    CK(A(&d_ncell, 1));
+    {
+      unsigned long long v = (unsigned long long)K.ncell;
+      CK(cudaMemcpy(d_ncell, &v, sizeof(v), cudaMemcpyHostToDevice));
+    }
+    Q.d_ncell = d_ncell;
+    CK(A(&d_gam, F));
+    CK(A(&d_pinf, F));
+    CK(cudaMemcpy(d_gam, K.gamma, sizeof(double) * F, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_pinf, K.pinf, sizeof(double) * F, cudaMemcpyHostToDevice));
     P.xb = 0;
     P.hb = 0;
     int rc = init_boundary();
@@ -755,8 +779,50 @@ struct Ctx : pgdg_ctx {
     timed("limiter", 1, [&] { Launch<D, R, EX>::limiter(K, P, st); });
     return PGDG_OK;
   }
+  int iface_download(double* in6, int8_t* mat2, int64_t cap, int64_t* n) override {
+    flush_prof();
+    CK(cudaStreamSynchronize(st));
+    *n = iface_last;
+    const int64_t m = std::min<int64_t>(cap, iface_last);
+    if (m > 0) {
+      CK(cudaMemcpy(in6, Q.in6, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(mat2, Q.mat, 2 * m, cudaMemcpyDeviceToHost));
+    }
+    return PGDG_OK;
+  }
+  int grow_queue(int64_t need) {
+    for (void* p : {(void*)Q.in6, (void*)Q.mat, (void*)Q.out3}) {
+      for (auto& a : allocs)
+        if (a == p) a = nullptr;
+      cudaFree(p);
+    }
+    Q.cap = need + need / 2;
+    CK(A(&Q.in6, 6 * (size_t)Q.cap));
+    CK(A(&Q.mat, 2 * (size_t)Q.cap));
+    CK(A(&Q.out3, 3 * (size_t)Q.cap));
+    return PGDG_OK;
+  }
   int grid_acc() override {
-    timed("grid_acc", 1, [&] { Launch<D, R, EX>::grid_acc(K, P, st); });
+    if (!iface_queue || EX) {
+      timed("grid_acc", 1, [&] { Launch<D, R, EX>::grid_acc(K, P, st); });
+      return PGDG_OK;
+    }
+    /* surrogate-seeded MGFM: queue the interface problems, solve them in one
+     * batch, then evaluate the residual with the queued ghost states */
+    int64_t n = 0;
+    timed("iface_gather", 6, [&] { n = Launch<D, R, EX>::iface_gather(K, P, Q, st); });
+    if (n < 0) {
+      int rc = grow_queue(-n);
+      if (rc) return rc;
+      timed("iface_gather", 6, [&] { n = Launch<D, R, EX>::iface_gather(K, P, Q, st); });
+    }
+    iface_last = n;
+    int rc = PGDG_OK;
+    timed("mgfm_seeded", 3, [&] {
+      rc = mgfm_seeded_run(net, Q.in6, Q.mat, d_gam, d_pinf, K.mgfm_variant, Q.out3, n, &P.cnt->mgfm_calls, st);
+    });
+    if (rc) return rc;
+    timed("grid_acc", 1, [&] { Launch<D, R, EX>::grid_acc_queued(K, P, Q, st); });
     return PGDG_OK;
   }
   int update_grid(int md) override {
@@ -875,11 +941,32 @@ int pgdg_set_iterate(pgdg_ctx* ctx, int64_t n) {
   return PGDG_OK;
 }
 int pgdg_set_max_v(pgdg_ctx* ctx, double mv) { return ctx->set_max_v(mv); }
-int pgdg_set_seed_mode(pgdg_ctx* ctx, int mode) {
-  ctx->seed_mode = mode;
+int pgdg_get_stats(pgdg_ctx* ctx, pgdg_stats* st) { return ctx->stats(st); }
+int pgdg_set_surrogate(pgdg_ctx* ctx, pgdg_mlp* net) {
+  if (net && ctx->precision == PGDG_PREC_FP64) {
+    ctx->err = "the seed surrogate is not used by the exact-order FP64 path";
+    return PGDG_EINVAL;
+  }
+  ctx->net = (void*)net;
+  ctx->iface_queue = net ? 1 : ctx->iface_queue;
   return PGDG_OK;
 }
-int pgdg_get_stats(pgdg_ctx* ctx, pgdg_stats* st) { return ctx->stats(st); }
+int pgdg_set_iface_queue(pgdg_ctx* ctx, int on) {
+  if (on && ctx->precision == PGDG_PREC_FP64) {
+    ctx->err = "the exact-order FP64 path solves interface problems inline";
+    return PGDG_EINVAL;
+  }
+  if (!on && ctx->net) {
+    ctx->err = "detach the seed surrogate first";
+    return PGDG_EINVAL;
+  }
+  ctx->iface_queue = on ? 1 : 0;
+  return PGDG_OK;
+}
+int pgdg_iface_download(pgdg_ctx* ctx, double* in6, int8_t* mat2, int64_t cap, int64_t* n) {
+  if (!in6 || !mat2 || !n || cap < 0) return PGDG_EINVAL;
+  return ctx->iface_download(in6, mat2, cap, n);
+}
 int pgdg_synchronize(pgdg_ctx* ctx) { return ctx->check(); }
 int pgdg_set_timestep(pgdg_ctx* ctx, double* dt, double* mv) { return ctx->set_timestep(dt, mv); }
 int pgdg_used_state_update(pgdg_ctx* ctx) { return ctx->used_state(); }

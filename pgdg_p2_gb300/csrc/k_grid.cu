@@ -532,9 +532,11 @@ __device__ __forceinline__ void flux_col(const R* Uu, const R* v, R Pp, int a, R
   Fc[U - 1] += v[a] * Pp;
 }
 
-template <int D, typename R, bool EX>
+/* MODE 0: MGFM solved inline; MODE 2: queue every interface problem (no flux
+ * work); MODE 3: read the ghost states of the interface problems from the queue */
+template <int D, typename R, bool EX, int MODE>
 __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int variant, double voli_d,
-                                                 double mij1, double mij2, double mij3) {
+                                                 double mij1, double mij2, double mij3, IfaceQ Q) {
   constexpr int U = D + 2, B = D + 1, NF = 2 * D, NQ = (D == 3) ? 4 : 2, NG = (D == 3) ? 8 : 4;
   const int64_t nc = K.ncell;
   const double gp[2] = {-1. / sqrt(3.), 1. / sqrt(3.)};
@@ -547,6 +549,13 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
     center<D>(K, idx, xc);
     const bool mirror_j = (idx[1] == K.N[1] - 1 || idx[1] == 0);
     const bool mirror_k = (D == 3) && (idx[2] == K.N[2] - 1 || idx[2] == 0);
+    int64_t qi = 0;
+    if constexpr (MODE != 0) {
+      if (Q.off[ci + 1] == Q.off[ci]) {
+        if constexpr (MODE == 2) continue;
+      }
+      qi = (int64_t)Q.off[ci];
+    }
     for (int ss = 0; ss < F; ss++) {
       if (P.cph[ss * nc + ci] != 1) continue;
       const R gs = (R)K.gamma[ss], pfs = (R)K.pinf[ss];
@@ -560,7 +569,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
       }
       /* volume integral, 2^D Gauss points */
       const R voli = (R)voli_d;
-      for (int g = 0; g < NG; g++) {
+      for (int g = 0; g < (MODE == 2 ? 0 : NG); g++) {
         int g1 = (D == 3) ? (g >> 2) : (g >> 1), g2 = (D == 3) ? ((g >> 1) & 1) : (g & 1), g3 = g & 1;
         R dp[3] = {(R)(gp[g1] * (K.ps[0] / 2)), (R)(gp[g2] * (K.ps[1] / 2)), (D == 3) ? (R)(gp[g3] * (K.ps[2] / 2)) : R(0)};
         const R gw = (D == 3) ? R(0.125) : R(0.25);
@@ -623,6 +632,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
             for (int s1 = 0; s1 < F; s1++) {
               const R aj = P.calph[s1 * nc + nb];
               if (aj == R(0)) continue;
+              if (MODE == 2 && s1 == ss) continue;
               R drj[3];
               for (int d = 0; d < D; d++) drj[d] = (R)(dpv[d] + fc.cen[d] - xn[d]);
               R Uj[U];
@@ -644,11 +654,32 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
               R vnj = v_j[a] * na;
               if (ss != s1) {
                 double gh[3];
-                int it = mgfm((double)vni, (double)vnj, (double)P_i, (double)P_j, (double)rho_i, (double)rho_j,
-                              K.gamma[ss], K.pinf[ss], K.gamma[s1], K.pinf[s1], variant, -1.0, gh);
-                ncall++;
-                nit += it;
-                if (it >= 50) nmax++;
+                if constexpr (MODE == 2) {
+                  const int64_t e = qi++;
+                  if (e < Q.cap) {
+                    double* q6 = Q.in6 + 6 * e;
+                    q6[0] = (double)vni;
+                    q6[1] = (double)vnj;
+                    q6[2] = (double)P_i;
+                    q6[3] = (double)P_j;
+                    q6[4] = (double)rho_i;
+                    q6[5] = (double)rho_j;
+                    Q.mat[2 * e] = (int8_t)ss;
+                    Q.mat[2 * e + 1] = (int8_t)s1;
+                  }
+                  continue;
+                } else if constexpr (MODE == 3) {
+                  const int64_t e = qi++;
+                  gh[0] = Q.out3[3 * e];
+                  gh[1] = Q.out3[3 * e + 1];
+                  gh[2] = Q.out3[3 * e + 2];
+                } else {
+                  int it = mgfm((double)vni, (double)vnj, (double)P_i, (double)P_j, (double)rho_i, (double)rho_j,
+                                K.gamma[ss], K.pinf[ss], K.gamma[s1], K.pinf[s1], variant, -1.0, gh);
+                  ncall++;
+                  nit += it;
+                  if (it >= 50) nmax++;
+                }
                 rho_j = (R)gh[0];
                 P_j = (R)gh[1];
                 vnj = (R)gh[2];
@@ -699,6 +730,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
               for (int b = 0; b < B; b++)
                 for (int u = 0; u < U; u++) DFn[b][u] += Fh[u] * Nb[b] * gw * aj;
             }
+          } else if (MODE == 2) {
           } else if (fc.bound == PGDG_BC_WALL) {
             for (int b = 0; b < B; b++) DFn[b][1 + a] += P_i * Nb[b] * gw;
           } else {
@@ -757,6 +789,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
         for (int b = 0; b < B; b++)
           for (int u = 0; u < U; u++) dc[u][b] += (-DFn[b][u] * na) * Sj;
       }
+      if constexpr (MODE == 2) continue;
       const R inv[4] = {R(1. / (voli_d + 1e-20)), R(1. / (mij1 + 1e-20)), R(1. / (mij2 + 1e-20)),
                         R(1. / (mij3 + 1e-20))};
       for (int u = 0; u < U; u++)
@@ -770,13 +803,72 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
   }
 }
 
+/* interface problems of each cell: present phase x interior face x quadrature
+ * point x other neighbour phase present (the MGFM calls of particle_flow.cpp:192-204) */
+template <int D, typename R, bool EX>
+__global__ void k_iface_count(CaseK K, DevPtrs<R> P, unsigned long long* cnt) {
+  const int64_t nc = K.ncell;
+  constexpr int NQ = (D == 3) ? 4 : 2;
+  GRID_STRIDE(ci, nc) {
+    unsigned long long n = 0;
+    if (P.cused[ci]) {
+      int idx[3];
+      cijk<D>(K, ci, idx);
+      for (int f = 0; f < 2 * D; f++) {
+        const int a = (f == 0 || f == 2) ? 1 : (f == 1 || f == 3) ? 0 : 2;
+        const int sg = (f == 0 || f == 3 || f == 4) ? -1 : 1;
+        int nb[3] = {idx[0], idx[1], idx[2]};
+        nb[a] += sg;
+        if (nb[a] < 0 || nb[a] >= K.N[a]) continue;
+        const int64_t cn = cidx3(K, nb[0], nb[1], nb[2]);
+        for (int ss = 0; ss < F; ss++) {
+          if (P.cph[ss * nc + ci] != 1) continue;
+          for (int s1 = 0; s1 < F; s1++)
+            if (s1 != ss && P.calph[s1 * nc + cn] != R(0)) n += NQ;
+        }
+      }
+    }
+    cnt[ci] = n;
+  }
+}
+template <typename R, bool EX>
+__global__ void k_iface_total(const unsigned long long* blk, int nblk, unsigned long long* off, int64_t nc) {
+  off[nc] = blk[nblk];
+}
+
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::grid_acc(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
   double voli = K.ps[0] * K.ps[1];
   if (D == 3) voli = voli * K.ps[2];
   double ps[3] = {K.ps[0] / 2, K.ps[1] / 2, K.ps[2] / 2};
   double m1 = (ps[0] * ps[0] / 3.) * voli, m2 = (ps[1] * ps[1] / 3.) * voli, m3 = (ps[2] * ps[2] / 3.) * voli;
-  k_grid_acc<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, m1, m2, m3);
+  IfaceQ Q{};
+  k_grid_acc<D, R, EX, 0><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, m1, m2, m3, Q);
+}
+
+template <int D, typename R, bool EX>
+int64_t Launch<D, R, EX>::iface_gather(const CaseK& K, const DevPtrs<R>& P, IfaceQ Q, cudaStream_t st) {
+  double voli = K.ps[0] * K.ps[1];
+  if (D == 3) voli = voli * K.ps[2];
+  k_iface_count<D, R, EX><<<grid_for(K.ncell, BLK), BLK, 0, st>>>(K, P, Q.off);
+  scan_u64(Q.off, Q.blk, Q.d_ncell, K.ncell, st);
+  const int nblk = (int)((K.ncell + 2047) / 2048);
+  k_iface_total<R, EX><<<1, 1, 0, st>>>(Q.blk, nblk, Q.off, K.ncell);
+  unsigned long long tot = 0;
+  cudaMemcpyAsync(&tot, Q.off + K.ncell, sizeof(tot), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  if ((int64_t)tot > Q.cap) return -(int64_t)tot;
+  k_grid_acc<D, R, EX, 2><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, 0, 0, 0, Q);
+  return (int64_t)tot;
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::grid_acc_queued(const CaseK& K, const DevPtrs<R>& P, IfaceQ Q, cudaStream_t st) {
+  double voli = K.ps[0] * K.ps[1];
+  if (D == 3) voli = voli * K.ps[2];
+  double ps[3] = {K.ps[0] / 2, K.ps[1] / 2, K.ps[2] / 2};
+  double m1 = (ps[0] * ps[0] / 3.) * voli, m2 = (ps[1] * ps[1] / 3.) * voli, m3 = (ps[2] * ps[2] / 3.) * voli;
+  k_grid_acc<D, R, EX, 3><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, m1, m2, m3, Q);
 }
 
 /* ------------------------------------------------------------------ */
@@ -895,6 +987,8 @@ void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out
   template void Launch<D, R, EX>::p2g(const CaseK&, const DevPtrs<R>&, cudaStream_t);              \
   template void Launch<D, R, EX>::limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \
   template void Launch<D, R, EX>::grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);         \
+  template int64_t Launch<D, R, EX>::iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t); \
+  template void Launch<D, R, EX>::grid_acc_queued(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t); \
   template void Launch<D, R, EX>::update_grid(const CaseK&, const DevPtrs<R>&, int, cudaStream_t); \
   template void Launch<D, R, EX>::totals(const CaseK&, const DevPtrs<R>&, double*, cudaStream_t);
 #ifdef PGDG_EXACT_TU

@@ -34,14 +34,3 @@ void mgfm_batched_launch(const double* in6, const int8_t* mat2, const double* ga
 
 }  // namespace pgdg
 
-extern "C" int pgdg_mgfm_batched(pgdg_ctx* ctx, const double* in6, const int8_t* mat2, const double* gam,
-                                 const double* pinf, int nmat, int variant, int seed_mode, double* out3,
-                                 int32_t* iters, int64_t n) {
-  (void)ctx;
-  if (n < 0 || !in6 || !mat2 || !gam || !pinf || !out3 || nmat < 1) return PGDG_EINVAL;
-  if (seed_mode != PGDG_SEED_PLAIN) return PGDG_EINVAL;
-  if (n == 0) return PGDG_OK;
-  pgdg::mgfm_batched_launch(in6, mat2, gam, pinf, variant, nullptr, out3, iters, n, 0);
-  cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
-}

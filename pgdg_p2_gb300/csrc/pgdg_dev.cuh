@@ -121,6 +121,18 @@ struct DevPtrs {
   int hb;           /* index of the current h buffer */
 };
 
+/* queue of interface Riemann problems of one stage (mixed path with the seed
+ * surrogate): off = exclusive per-cell offsets (ncell + 1) */
+struct IfaceQ {
+  double* in6;
+  int8_t* mat;
+  double* out3;
+  unsigned long long* off;
+  unsigned long long* blk;
+  const unsigned long long* d_ncell;
+  int64_t cap;
+};
+
 /* ---------------- cell ids ---------------- */
 template <int D>
 __device__ __forceinline__ int64_t cidx(const CaseK& K, const int* pos) {
@@ -183,6 +195,9 @@ struct Launch {
   static void p2g(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  /* queued variant: returns the number of interface problems (negative: over capacity) */
+  static int64_t iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t);
+  static void grid_acc_queued(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t);
   static void update_grid(const CaseK&, const DevPtrs<R>&, int md, cudaStream_t);
   static void totals(const CaseK&, const DevPtrs<R>&, double* d_out6, cudaStream_t);
   /* k_g2p.cu */
@@ -191,6 +206,11 @@ struct Launch {
   static void g2p(const CaseK&, const DevPtrs<R>&, int md, int xs, int x0, int xn, int hn, cudaStream_t);
   static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, cudaStream_t);
 };
+
+/* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls, iterations, cap hits) */
+struct pgdg_mlp_fwd;
+int mgfm_seeded_run(void* net, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
+                    int variant, double* out3, int64_t n, unsigned long long* stats, cudaStream_t st);
 
 /* shared helpers used by several translation units */
 int grid_for(int64_t n, int block);

@@ -160,9 +160,18 @@ PGDG_HD int mgfm(double ul, double ur, double pl, double pr, double rhol, double
     double dp = ddiv(-f1, jac);
     double cap = dmul(0.6, pstar);
     if (fabs(dp) > cap) dp = copysign(cap, dp);
+    const double pold = pstar;
     pstar = dadd(pstar, dp);
     pstar = amax1(pstar, 1e-8);
     nn++;
+    /* every quantity of an iteration is a function of pstar alone: once an
+     * unconverged iterate repeats (the 1e-8 floor of a problem without a
+     * positive root) the remaining iterations up to the cap reproduce it bit
+     * for bit, so leave with the cap count the full loop would report */
+    if (pstar == pold && fabs(f1) > tol) {
+      nn = 50;
+      break;
+    }
   } while (fabs(f1) > tol && nn < 50);
   if (variant != 0) usl = dsub(ul, ddiv(dsub(pstar, pl), Wl));
   out[0] = rhols;

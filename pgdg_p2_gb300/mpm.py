@@ -15,7 +15,7 @@ import os
 import numpy as np
 
 from . import build as _build
-from .abi import (PREC_FP64, PREC_MIXED, SEED_MLP, SEED_PLAIN, Cells, Particles, PgdgError,  # noqa: F401
+from .abi import (PREC_FP64, PREC_MIXED, Cells, Particles, PgdgError,  # noqa: F401
                   check, declare_case_builder, pgdg_case, pgdg_cells, pgdg_particles, pgdg_stats)
 
 _lib = None
@@ -51,7 +51,6 @@ def lib():
         L.pgdg_set_dt.argtypes = [vp, C.c_double]
         L.pgdg_set_iterate.argtypes = [vp, C.c_int64]
         L.pgdg_set_max_v.argtypes = [vp, C.c_double]
-        L.pgdg_set_seed_mode.argtypes = [vp, C.c_int]
         L.pgdg_get_stats.argtypes = [vp, P(pgdg_stats)]
         L.pgdg_set_timestep.argtypes = [vp, P(C.c_double), P(C.c_double)]
         L.pgdg_update_grid.argtypes = [vp, C.c_int]
@@ -63,8 +62,19 @@ def lib():
         L.pgdg_profile_read.argtypes = [vp, C.c_char_p, C.c_int, P(C.c_double), P(C.c_int64), C.c_int, P(C.c_int)]
         L.pgdg_launch_count.argtypes = [vp, P(C.c_int64)]
         L.pgdg_time_advance.argtypes = [vp, C.c_int, P(C.c_double)]
-        L.pgdg_mgfm_batched.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
-                                        C.c_int, C.c_void_p, C.c_void_p, C.c_int64]
+        L.pgdg_mgfm_batched.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int64]
+        L.pgdg_surrogate_create.argtypes = [C.c_int, P(vp)]
+        L.pgdg_surrogate_destroy.argtypes = [vp]
+        L.pgdg_surrogate_num_params.restype = C.c_int
+        L.pgdg_surrogate_set_params.argtypes = [vp, P(C.c_float)]
+        L.pgdg_surrogate_get_params.argtypes = [vp, P(C.c_float)]
+        L.pgdg_surrogate_features.argtypes = [vp, vp, vp, vp, vp, C.c_int64]
+        L.pgdg_surrogate_forward.argtypes = [vp, vp, vp, C.c_int64]
+        L.pgdg_surrogate_gradients.argtypes = [vp, vp, vp, C.c_int64, P(C.c_float), P(C.c_double)]
+        L.pgdg_surrogate_train_step.argtypes = [vp, vp, vp, C.c_int64, C.c_float, P(C.c_double)]
+        L.pgdg_set_surrogate.argtypes = [vp, vp]
+        L.pgdg_set_iface_queue.argtypes = [vp, C.c_int]
+        L.pgdg_iface_download.argtypes = [vp, vp, vp, C.c_int64, P(C.c_int64)]
         _lib = L
     return _lib
 
@@ -195,8 +205,23 @@ class MPM:
     def set_max_v(self, mv):
         self._ck(lib().pgdg_set_max_v(self.h, float(mv)), "set_max_v")
 
-    def set_seed_mode(self, mode):
-        self._ck(lib().pgdg_set_seed_mode(self.h, int(mode)), "set_seed_mode")
+    def set_surrogate(self, net):
+        """Seed every interface MGFM solve of the mixed step with `net` (None: plain)."""
+        self._ck(lib().pgdg_set_surrogate(self.h, net.h if net is not None else None), "set_surrogate")
+
+    def set_iface_queue(self, on):
+        """Solve each stage's interface problems as one batch (mixed / FP64_FMA paths)."""
+        self._ck(lib().pgdg_set_iface_queue(self.h, 1 if on else 0), "set_iface_queue")
+
+    def iface_problems(self):
+        """The last stage's queued interface problems: (in6 [n,6], mat2 [n,2])."""
+        n = C.c_int64()
+        z6, z2 = np.zeros((1, 6)), np.zeros((1, 2), np.int8)
+        self._ck(lib().pgdg_iface_download(self.h, z6.ctypes.data, z2.ctypes.data, 0, C.byref(n)), "iface_download")
+        in6, mat = np.zeros((max(n.value, 1), 6)), np.zeros((max(n.value, 1), 2), np.int8)
+        self._ck(lib().pgdg_iface_download(self.h, in6.ctypes.data, mat.ctypes.data, n.value, C.byref(n)),
+                 "iface_download")
+        return in6[:n.value], mat[:n.value]
 
     def stats(self):
         s = pgdg_stats()

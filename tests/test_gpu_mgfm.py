@@ -20,7 +20,7 @@ def _run_gpu(M, in6, mat, gam, pinf, variant=0):
     it = torch.zeros(len(in6), dtype=torch.int32, device=dev)
     torch.cuda.synchronize()
     rc = M.lib().pgdg_mgfm_batched(None, t_in.data_ptr(), t_m.data_ptr(), t_g.data_ptr(), t_p.data_ptr(), len(gam),
-                                   variant, 0, out.data_ptr(), it.data_ptr(), len(in6))
+                                   variant, out.data_ptr(), it.data_ptr(), len(in6))
     assert rc == 0
     torch.cuda.synchronize()
     return out.cpu().numpy(), it.cpu().numpy()

@@ -1,0 +1,165 @@
+"""MGFM seed surrogate on the device: features, forward pass and gradients
+against the NumPy FP64 restatement; the seeded batched solve against the plain
+one; the interface-queued residual against the FP64 oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from tests import mlp_ref as R
+from tests.gpu_helpers import conserved_l1
+
+pytestmark = pytest.mark.gpu
+
+
+def _cuda(a, dtype):
+    import torch
+    return torch.tensor(np.ascontiguousarray(a), dtype=dtype, device="cuda:0")
+
+
+def _c5(n, seed):
+    from pgdg_p2_gb300 import surrogate as S
+    in6, mat = S.c5_problems(n, seed=seed)
+    ps, us, has = S.exact_roots(in6, mat, S.C5_GAMMA, S.C5_PINF)
+    X, _, _, _ = S.features_np(in6, mat, S.C5_GAMMA, S.C5_PINF)
+    T = S.targets_np(in6, mat, S.C5_GAMMA, S.C5_PINF, ps, us)
+    return in6, mat, X[has], T[has], has
+
+
+def test_features_match_host(gpu_mod):
+    import torch
+    from pgdg_p2_gb300 import surrogate as S
+    in6, mat = S.c5_problems(8192, seed=7)
+    X = torch.zeros((len(in6), S.NI), dtype=torch.float32, device="cuda:0")
+    args = [_cuda(in6, torch.float64), _cuda(mat, torch.int8), _cuda(S.C5_GAMMA, torch.float64),
+            _cuda(S.C5_PINF, torch.float64)]
+    torch.cuda.synchronize()
+    assert gpu_mod.lib().pgdg_surrogate_features(*[a.data_ptr() for a in args], X.data_ptr(), len(in6)) == 0
+    torch.cuda.synchronize()
+    Xh, _, _, _ = S.features_np(in6, mat, S.C5_GAMMA, S.C5_PINF)
+    np.testing.assert_allclose(X.cpu().numpy(), Xh, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("bf16", [False, True])
+def test_forward_matches_numpy(gpu_mod, bf16):
+    import torch
+    from pgdg_p2_gb300 import surrogate as S
+    _, _, X, T, _ = _c5(6000, 8)
+    p = S.init_params(X, T, seed=3)
+    net = S.Surrogate(p, bf16=bf16)
+    Xd = _cuda(X, torch.float32)
+    Y = torch.zeros((len(X), S.NO), dtype=torch.float32, device="cuda:0")
+    torch.cuda.synchronize()
+    assert gpu_mod.lib().pgdg_surrogate_forward(net.h, Xd.data_ptr(), Y.data_ptr(), len(X)) == 0
+    torch.cuda.synchronize()
+    Yr, _ = R.forward(p, X, bf16)
+    # FP32 accumulation and tanhf against FP64: 2e-5 relative
+    assert np.all(np.abs(Y.cpu().numpy() - Yr) <= 2e-5 * (1 + np.abs(Yr)))
+    net.close()
+
+
+@pytest.mark.parametrize("bf16", [False, True])
+def test_gradients_match_numpy(gpu_mod, bf16):
+    import torch
+    from pgdg_p2_gb300 import surrogate as S
+    _, _, X, T, _ = _c5(6000, 9)
+    p = S.init_params(X, T, seed=4)
+    net = S.Surrogate(p, bf16=bf16)
+    Xd, Td = _cuda(X, torch.float32), _cuda(T, torch.float32)
+    g = np.zeros(S.NPARAM, np.float32)
+    loss = C.c_double()
+    torch.cuda.synchronize()
+    assert gpu_mod.lib().pgdg_surrogate_gradients(net.h, Xd.data_ptr(), Td.data_ptr(), len(X),
+                                                  g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)) == 0
+    lr, gr = R.loss_grad(p, X, T, bf16)
+    assert abs(loss.value - lr) <= 1e-5 * lr
+    # FP32 sums over the batch against FP64: 1e-4 relative in norm, per layer
+    o = 0
+    for a, b in R.SHAPES:
+        for size in (a * b, a):
+            sl = slice(o, o + size)
+            assert np.linalg.norm(g[sl] - gr[sl]) <= 1e-4 * np.linalg.norm(gr[sl]) + 1e-9, (a, b, size)
+            o += size
+    net.close()
+
+
+def test_training_reduces_loss(gpu_mod):
+    from pgdg_p2_gb300 import surrogate as S
+    _, _, X, T, _ = _c5(40000, 10)
+    p, hist = S.train(X, T, steps=300, batch=4096, lr=2e-3, seed=1)
+    assert np.all(np.isfinite(p))
+    assert hist[-1][1] < 0.5 * hist[0][1], hist
+
+
+def _check_seeded(in6, mat, gam, pinf, net, variant=0):
+    from pgdg_p2_gb300 import surrogate as S
+    op, ip = S.mgfm_gpu(in6, mat, gam, pinf, None, variant)
+    osd, isd = S.mgfm_gpu(in6, mat, gam, pinf, net, variant)
+    conv = ip < 50
+    tol = np.maximum(1e-8, 1e-3 * np.abs(in6[:, 0] - in6[:, 1]))
+    # both solves stop within the Newton tolerance of the same root
+    assert np.all(np.abs(osd[conv, 2] - op[conv, 2]) <= 2 * tol[conv])
+    rel = np.abs(osd[conv, 1] - op[conv, 1]) / op[conv, 1]
+    assert rel.max() <= 5e-3 and np.quantile(rel, 0.99) <= 1e-4
+    # problems without a root take the plain path unchanged
+    assert osd[~conv].tobytes() == op[~conv].tobytes()
+    return ip, isd, conv
+
+
+def test_seeded_solve_untrained_falls_back(gpu_mod):
+    from pgdg_p2_gb300 import surrogate as S
+    in6, mat, X, T, _ = _c5(1 << 15, 11)
+    net = S.Surrogate(S.init_params(X, T, seed=5))
+    _check_seeded(in6, mat, S.C5_GAMMA, S.C5_PINF, net)
+    net.close()
+
+
+def test_seeded_solve_trained_saves_iterations(gpu_mod):
+    from pgdg_p2_gb300 import surrogate as S
+    p = S.load_default()
+    assert p is not None, "trained weights missing"
+    in6, mat = S.c5_problems(1 << 16, seed=5)
+    net = S.Surrogate(p)
+    ip, isd, conv = _check_seeded(in6, mat, S.C5_GAMMA, S.C5_PINF, net)
+    # Newton iterations on the problems with a root: at least 30% fewer
+    assert isd[conv].mean() <= 0.7 * ip[conv].mean(), (isd[conv].mean(), ip[conv].mean())
+    net.close()
+
+
+@pytest.mark.parametrize("cid,grid,steps", [(3, (96, 24, 24), 10), (4, (128, 128), 10)])
+def test_queued_residual_vs_oracle(gpu_mod, oracle_mod, cid, grid, steps):
+    """Mixed step with the interface queue (and the trained seed) against the
+    FP64 oracle, with the accuracy gate of the mixed path (1e-3 relative L1)."""
+    from pgdg_p2_gb300 import surrogate as S
+    from pgdg_p2_gb300.abi import PREC_MIXED
+    M, O = gpu_mod, oracle_mod
+    cs, p, c = M.make_case(cid, grid)
+    g = M.MPM(cs, PREC_MIXED)
+    params = S.load_default()
+    net = S.Surrogate(params) if params is not None else None
+    if net is not None:
+        g.set_surrogate(net)
+    else:
+        g.set_iface_queue(True)
+    o = O.Oracle(cs)
+    for x in (g, o):
+        x.upload_particles(p)
+        x.upload_cells(c)
+    nq = 0
+    for s in range(1, steps + 1):
+        dt, mv = o.Set_timestep()
+        g.Set_timestep()
+        g.set_dt(dt)
+        g.set_max_v(mv)
+        g.set_iterate(s)
+        o.set_iterate(s)
+        g.MPM_run_simulation(s)
+        o.MPM_run_simulation(s)
+        in6, mat = g.iface_problems()
+        nq += len(in6)
+        assert set(np.unique(mat)) <= {0, 1}
+    g.sync()
+    assert nq > 0
+    per, mom = conserved_l1(cs, g.download_cells(), o.download_cells())
+    tol = 1e-3 if cid != 4 else 2e-3
+    assert per[0] <= tol and per[-1] <= tol and max(mom) <= tol, (per, mom)

@@ -183,6 +183,9 @@ struct Ctx : pgdg_ctx {
       K.gamma[s] = cs.gamma[s];
       K.pinf[s] = cs.pinf[s];
       K.ini_rho[s] = cs.ini_rho[s];
+      const bool shift = sizeof(R) == 4 && cs.pinf[s] != 0.0;
+      K.eshift[s] = shift ? cs.gamma[s] * cs.pinf[s] / (cs.gamma[s] - 1.0) : 0.0;
+      K.pinf_eos[s] = shift ? 0.0 : cs.pinf[s];
     }
     K.inlet_rho = cs.inlet_rho;
     for (int d = 0; d < 3; d++) K.inlet_u[d] = cs.inlet_u[d];
@@ -379,7 +382,11 @@ struct Ctx : pgdg_ctx {
         rhov[d * n + i] = (R)pp->rhov[3 * i + d];
       }
       vol[i] = (R)pp->vol[i]; mass[i] = (R)pp->mass[i]; h[i] = (R)pp->h[i]; Pp[i] = (R)pp->P[i];
-      rho[i] = (R)pp->rho[i]; E[i] = (R)pp->E[i]; c[i] = (R)pp->c[i];
+      rho[i] = (R)pp->rho[i]; c[i] = (R)pp->c[i];
+      {
+        const int s = pp->phase[i] - 1;
+        E[i] = (R)(s >= 0 && s < F && K.eshift[s] != 0.0 ? pp->E[i] - K.eshift[s] : pp->E[i]);
+      }
       for (int t = 0; t < NS; t++) sl[t * n + i] = pp->slope ? (R)pp->slope[NS * i + t] : R(0);
       phase[i] = (int8_t)pp->phase[i];
       mark[i] = pp->mark_in ? (int8_t)pp->mark_in[i] : 0;
@@ -481,7 +488,10 @@ struct Ctx : pgdg_ctx {
       if (pp->h) pp->h[i] = h[s];
       if (pp->P) pp->P[i] = Pp[s];
       if (pp->rho) pp->rho[i] = rho[s];
-      if (pp->E) pp->E[i] = E[s];
+      if (pp->E) {
+        const int f = phase[s] - 1;
+        pp->E[i] = (f >= 0 && f < F && K.eshift[f] != 0.0) ? (double)E[s] + K.eshift[f] : (double)E[s];
+      }
       if (pp->c) pp->c[i] = c[s];
       if (pp->slope)
         for (int t = 0; t < NS; t++) pp->slope[NS * i + t] = sl[t * ns + s];
@@ -507,12 +517,14 @@ struct Ctx : pgdg_ctx {
         int64_t q = ci * F + s;
         rho[s * nc + ci] = (R)cc->rho[q];
         for (int d = 0; d < D; d++) rhov[(s * D + d) * nc + ci] = (R)cc->rhov[q * 3 + d];
-        E[s * nc + ci] = (R)cc->E[q];
+        E[s * nc + ci] = (R)(K.eshift[s] != 0.0 ? cc->E[q] - K.eshift[s] : cc->E[q]);
         c[s * nc + ci] = (R)cc->c[q];
         ac[s * nc + ci] = cc->ac ? (R)cc->ac[q] : R(0);
         alph[s * nc + ci] = (R)cc->alph[q];
         for (int t = 0; t < U * B; t++) {
-          coef[(s * U * B + t) * nc + ci] = (R)cc->coef[q * U * B + t];
+          coef[(s * U * B + t) * nc + ci] = (R)((t == (U - 1) * B && K.eshift[s] != 0.0)
+                                                    ? cc->coef[q * U * B + t] - K.eshift[s]
+                                                    : cc->coef[q * U * B + t]);
           dco[(s * U * B + t) * nc + ci] = cc->dcoef ? (R)cc->dcoef[q * U * B + t] : R(0);
         }
         for (int u = 0; u < U; u++) lim[(s * U + u) * nc + ci] = cc->lim_u ? (R)cc->lim_u[q * U + u] : R(1);
@@ -573,11 +585,15 @@ struct Ctx : pgdg_ctx {
         int64_t q = ci * F + s;
         if (co->rho) co->rho[q] = rho[s * nc + ci];
         if (co->rhov) for (int d = 0; d < 3; d++) co->rhov[q * 3 + d] = d < D ? (double)rhov[(s * D + d) * nc + ci] : 0.0;
-        if (co->E) co->E[q] = E[s * nc + ci];
+        if (co->E) co->E[q] = K.eshift[s] != 0.0 ? (double)E[s * nc + ci] + K.eshift[s] : (double)E[s * nc + ci];
         if (co->c) co->c[q] = c[s * nc + ci];
         if (co->ac) co->ac[q] = ac[s * nc + ci];
         if (co->alph) co->alph[q] = alph[s * nc + ci];
-        if (co->coef) for (int t = 0; t < U * B; t++) co->coef[q * U * B + t] = coef[(s * U * B + t) * nc + ci];
+        if (co->coef)
+          for (int t = 0; t < U * B; t++)
+            co->coef[q * U * B + t] = (t == (U - 1) * B && K.eshift[s] != 0.0)
+                                          ? (double)coef[(s * U * B + t) * nc + ci] + K.eshift[s]
+                                          : (double)coef[(s * U * B + t) * nc + ci];
         if (co->dcoef) for (int t = 0; t < U * B; t++) co->dcoef[q * U * B + t] = dco[(s * U * B + t) * nc + ci];
         if (co->lim_u) for (int u = 0; u < U; u++) co->lim_u[q * U + u] = lim[(s * U + u) * nc + ci];
         if (co->ph_state) co->ph_state[q] = ph[s * nc + ci];
@@ -819,7 +835,7 @@ struct Ctx : pgdg_ctx {
     iface_last = n;
     int rc = PGDG_OK;
     timed("mgfm_seeded", 3, [&] {
-      rc = mgfm_seeded_run(net, Q.in6, Q.mat, d_gam, d_pinf, K.mgfm_variant, Q.out3, n, &P.cnt->mgfm_calls, st);
+      rc = mgfm_seeded_run(net, Q.in6, Q.mat, d_gam, d_pinf, K.mgfm_variant, Q.out3, nullptr, n, &P.cnt->mgfm_calls, st);
     });
     if (rc) return rc;
     timed("grid_acc", 1, [&] { Launch<D, R, EX>::grid_acc_queued(K, P, Q, st); });

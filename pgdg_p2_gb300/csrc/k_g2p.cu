@@ -78,8 +78,8 @@ __global__ void __launch_bounds__(128) k_g2p(CaseK K, DevPtrs<R> P, int md, int 
       sq = (k == 0) ? v[k] * v[k] : sq + v[k] * v[k];
     }
     const R g = (R)K.gamma[ss], pf = (R)K.pinf[ss];
-    R Pp = eos_p<R>(E - R(0.5) * rho * sq, g, pf);
-    R c = rsqrt_<R>(g * (pf + Pp) / rho);
+    R Pp = eos_p<R>(E - R(0.5) * rho * sq, g, (R)K.pinf_eos[ss]);
+    R c = sqrt_r<R>(g * (pf + Pp) / rho);
     bool fb = (Pp < R(-0.05) * pf || rho < R(0));
     for (int t = 0; t < U; t++)
       for (int b = 0; b < D; b++)
@@ -166,18 +166,26 @@ struct PstSmem {
   R* bhi;        /* D * nsc */
   V4* ent;       /* cap: (x, y, z | slot) of each staged particle at the stage start */
   unsigned short* buf; /* PST_BUF x PST_THREADS queued member entries */
-  int lo[3], n[3], nsc, cap, maxcnt;
+  /* mixed / FMA paths: the entries of each row of cells along the last axis
+   * (z in 3D, y in 2D) are sorted by that coordinate; ecell holds each entry's
+   * cell offset along the row, rlo/rhi the row's bounds in the other axes */
+  unsigned char* ecell; /* cap */
+  R* rlo;        /* 2 * nrow */
+  R* rhi;        /* 2 * nrow */
+  int lo[3], n[3], nsc, nrow, cap, maxcnt;
 };
 
 template <int D, typename R>
-__host__ __device__ inline size_t pst_smem_bytes(int nsc, int cap) {
+__host__ __device__ inline size_t pst_smem_bytes(int nsc, int nrow, int cap) {
   size_t b = sizeof(int) * (size_t)(3 * nsc + 1);
   b = (b + 31) / 32 * 32;
   b += sizeof(R) * (size_t)(2 * D * nsc);
   b = (b + 31) / 32 * 32;
   b += 4 * sizeof(R) * (size_t)cap;
   b += sizeof(unsigned short) * (size_t)PST_BUF * PST_THREADS;
-  return b + 64;
+  b += sizeof(R) * (size_t)(4 * nrow);
+  b += (size_t)cap;
+  return b + 128;
 }
 
 /* per-particle constants and accumulators of the shifting sum */
@@ -213,7 +221,7 @@ struct PstPart {
       R t = xsp[d] - xsq[d];
       dd = (d == 0) ? t * t : dd + t * t;
     }
-    if constexpr (EX) return rsqrt_<R>(dd) <= hs_p * R(CUT_OFF); /* get_distance <= h*CUT_OFF */
+    if constexpr (EX) return sqrt_r<R>(dd) <= hs_p * R(CUT_OFF); /* get_distance <= h*CUT_OFF */
     else return dd <= lim2;
   }
 
@@ -228,7 +236,7 @@ struct PstPart {
     if (d2 == R(0)) return;
     R s, q, q3, Wij, aw, rr;
     if constexpr (EX) {
-      R dist = rsqrt_<R>(d2);
+      R dist = sqrt_r<R>(d2);
       s = dist / hh;
       if (!(s < R(2))) return; /* W and dW vanish beyond the support */
       q = R(1.) - R(0.5) * s;
@@ -238,7 +246,7 @@ struct PstPart {
       rr = Wij / W_dp;
     } else {
       if constexpr (sizeof(R) == 4) s = d2 * rsqrtf(d2) * inv_hh;
-      else s = rsqrt_<R>(d2) * inv_hh;
+      else s = sqrt_r<R>(d2) * inv_hh;
       if (!(s < R(2))) return;
       q = R(1.) - R(0.5) * s;
       q3 = (q * q) * q;
@@ -344,36 +352,48 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
       }
     };
     if constexpr (!EX) {
-      /* mixed / FMA paths: each (i, j) row of cells is one contiguous run of
-       * staged entries; trim it to the cells whose bounding box meets the 2h
-       * sphere in z and skip rows whose x/y extent misses it.  Boundary particles
-       * follow in a second pass (the summation order only affects rounding). */
-      const R rr2 = lim2m * rsqrt_<R>(lim2m);
-      const int zl = lo[2] - sm->lo[2], zh = hi[2] - sm->lo[2];
+      /* mixed / FMA paths: for each row of cells along the last axis whose
+       * bounds in the other axes come within 2h, only the entries whose row
+       * coordinate lies within the sphere's chord are tested (binary search in
+       * the sorted row); the cell tag keeps the scan to the particle's
+       * +-rad2 cell window.  Boundary particles follow in a second pass (the
+       * summation order only affects rounding). */
+      constexpr int RA = D - 1;
+      const int clo = lo[RA] - sm->lo[RA], chi = hi[RA] - sm->lo[RA];
+      const R zp = pp.xsp[RA];
+      const int t1 = (D == 3) ? hi[1] : lo[1];
       for (int t = lo[0]; t <= hi[0]; t++)
-        for (int s = lo[1]; s <= hi[1]; s++) {
-          const int lr = ((t - sm->lo[0]) * sm->n[1] + (s - sm->lo[1])) * sm->n[2];
-          int f = zl, g = zh;
-          if (D == 3) {
-            const R zp = pp.xsp[2];
-            while (f <= g && !(sm->bhi[2 * sm->nsc + lr + f] >= zp - rr2)) f++;
-            while (g >= f && !(sm->blo[2 * sm->nsc + lr + g] <= zp + rr2)) g--;
+        for (int u = lo[1]; u <= t1; u++) {
+          const int row = (D == 3) ? (t - sm->lo[0]) * sm->n[1] + (u - sm->lo[1]) : (t - sm->lo[0]);
+          R dxy = R(0);
+          for (int d = 0; d < D - 1; d++) {
+            R a = sm->rlo[2 * row + d] - pp.xsp[d], b = pp.xsp[d] - sm->rhi[2 * row + d];
+            R w = a > b ? a : b;
+            if (w > R(0)) dxy += w * w;
           }
-          if (f <= g) {
-            R mx = R(0);
-            for (int d = 0; d < 2; d++) {
-              R a = R(1e30), b = R(-1e30);
-              for (int k = f; k <= g; k++) {
-                a = fmin(a, sm->blo[d * sm->nsc + lr + k]);
-                b = fmax(b, sm->bhi[d * sm->nsc + lr + k]);
-              }
-              R u = a - pp.xsp[d], v = pp.xsp[d] - b;
-              R w = u > v ? u : v;
-              if (w > R(0)) mx += w * w;
+          if (dxy <= lim2m) {
+            const R w = sqrt_r<R>(lim2m - dxy); /* half chord of the 2h sphere */
+            const R za = zp - w, zb = zp + w;
+            const int rl = row * sm->n[RA];
+            int e = sm->off[rl], e1 = sm->off[rl + sm->n[RA]];
+            int hi_e = e1;
+            while (e < hi_e) {   /* first entry with coordinate >= za */
+              const int m = (e + hi_e) >> 1;
+              const R zm = (RA == 2) ? sm->ent[m].z : sm->ent[m].y;
+              if (zm < za) e = m + 1;
+              else hi_e = m;
             }
-            if (mx <= lim2m) {
-              const int e0 = sm->off[lr + f], e1 = sm->off[lr + g + 1];
-              for (int e = e0; e < e1; e++) queue(e);
+            for (; e < e1; e++) {
+              const auto v = sm->ent[e];
+              const R zv = (RA == 2) ? v.z : v.y;
+              if (zv > zb) break;
+              const int ce = sm->ecell[e];
+              if (ce < clo || ce > chi) continue;
+              R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
+              if (pp.member(xsq)) {
+                if (nbuf == PST_BUF) flush();
+                sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
+              }
             }
           }
           if (__any_sync(__activemask(), nbuf >= PST_BUF / 2)) flush();
@@ -479,7 +499,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
     s1 = (d == 0) ? dx1[d] * dx1[d] : s1 + dx1[d] * dx1[d];
     s2 = (d == 0) ? dx2[d] * dx2[d] : s2 + dx2[d] * dx2[d];
   }
-  R dis0 = rsqrt_<R>(s0), dis1 = rsqrt_<R>(s1), dis2 = rsqrt_<R>(s2);
+  R dis0 = sqrt_r<R>(s0), dis1 = sqrt_r<R>(s1), dis2 = sqrt_r<R>(s2);
   R l0 = amin1(px / R(10), dis0) / (dis0 + R(1e-20));
   R l1 = amin1(px / R(10), dis1) / (dis1 + R(1e-20));
   R l2 = amin1(px / R(2), dis2) / (dis2 + R(1e-20));
@@ -532,6 +552,10 @@ __global__ void __launch_bounds__(PST_THREADS, 2) k_pst(CaseK K, DevPtrs<R> P, i
   o = (o + 31) / 32 * 32;
   sm.ent = reinterpret_cast<V4*>(smem_raw + o);
   sm.buf = reinterpret_cast<unsigned short*>(sm.ent + cap);
+  sm.nrow = (D == 3) ? sm.n[0] * sm.n[1] : sm.n[0];
+  sm.rlo = reinterpret_cast<R*>(sm.buf + (size_t)PST_BUF * PST_THREADS);
+  sm.rhi = sm.rlo + 2 * sm.nrow;
+  sm.ecell = reinterpret_cast<unsigned char*>(sm.rhi + 2 * sm.nrow);
   __shared__ int s_total, s_maxcnt;
   for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
     int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
@@ -600,6 +624,46 @@ __global__ void __launch_bounds__(PST_THREADS, 2) k_pst(CaseK K, DevPtrs<R> P, i
       }
     }
     __syncthreads();
+    if constexpr (!EX) {
+      /* one thread per row: tag entries with their cell offset along the row,
+       * insertion-sort them by the row coordinate (ties by slot), and record
+       * the row's bounds in the other axes */
+      constexpr int RA = D - 1;
+      const int nr = sm.n[RA];
+      for (int row = threadIdx.x; row < sm.nrow; row += blockDim.x) {
+        const int l0 = row * nr;
+        for (int k = 0; k < nr; k++)
+          for (int e = sm.off[l0 + k]; e < sm.off[l0 + k + 1]; e++) sm.ecell[e] = (unsigned char)k;
+        const int e0 = sm.off[l0], e1 = sm.off[l0 + nr];
+        for (int i = e0 + 1; i < e1; i++) {
+          const V4 v = sm.ent[i];
+          const unsigned char cv = sm.ecell[i];
+          const R key = (RA == 2) ? v.z : v.y;
+          const int sv = slot_of<R>(v.w);
+          int j = i - 1;
+          while (j >= e0) {
+            const V4 u = sm.ent[j];
+            const R ku = (RA == 2) ? u.z : u.y;
+            if (ku < key || (ku == key && slot_of<R>(u.w) < sv)) break;
+            sm.ent[j + 1] = u;
+            sm.ecell[j + 1] = sm.ecell[j];
+            j--;
+          }
+          sm.ent[j + 1] = v;
+          sm.ecell[j + 1] = cv;
+        }
+        for (int d = 0; d < D - 1; d++) {
+          R a = R(1e30), b = R(-1e30);
+          for (int k = 0; k < nr; k++) {
+            a = fmin(a, sm.blo[d * sm.nsc + l0 + k]);
+            b = fmax(b, sm.bhi[d * sm.nsc + l0 + k]);
+          }
+          sm.rlo[2 * row + d] = a;
+          sm.rhi[2 * row + d] = b;
+        }
+      }
+      __syncthreads();
+    }
   }
   /* the brick's own particles */
   const int nbc = bdim[0] * bdim[1] * bdim[2];
@@ -640,12 +704,13 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
   const int r = K.rad2;
   const int nsc = (BK::B0 + 2 * r) * (BK::B1 + 2 * r) * (D == 3 ? BK::B2 + 2 * r : 1);
   const int ppc = (D == 3) ? 8 : 4;
+  const int nrow = (D == 3) ? (BK::B0 + 2 * r) * (BK::B1 + 2 * r) : (BK::B0 + 2 * r);
   int cap = nsc * ppc * 5 / 4;
   if (cap > 65535) cap = 65535;
-  size_t bytes = pst_smem_bytes<D, R>(nsc, cap);
+  size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap);
   while (bytes > 220 * 1024 && cap > 256) {
     cap = cap * 3 / 4;
-    bytes = pst_smem_bytes<D, R>(nsc, cap);
+    bytes = pst_smem_bytes<D, R>(nsc, nrow, cap);
   }
   static bool attr_set = false;
   if (!attr_set) {

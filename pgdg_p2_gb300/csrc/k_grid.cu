@@ -117,11 +117,11 @@ __global__ void k_dt_reduce(CaseK K, DevPtrs<R> P, int by_cells) {
       if (!P.cused[ci]) continue;
       R sq = P.cv[ci] * P.cv[ci];
       for (int k = 1; k < D; k++) sq = sq + P.cv[k * nc + ci] * P.cv[k * nc + ci];
-      R U = rsqrt_<R>(sq);
+      R U = sqrt_r<R>(sq);
       R c12 = amax1(P.cc[ci], P.cc[nc + ci]);
       R a12 = amax1(P.cac[ci], P.cac[nc + ci]);
       R t = R(K.cfl) * ds / (c12 + U);
-      R tmp = R(K.cfl) * rsqrt_<R>(ds / a12);
+      R tmp = R(K.cfl) * sqrt_r<R>(ds / a12);
       t = amin1(t, tmp);
       tmin = fmin(tmin, (double)t);
       vmax = fmax(vmax, (double)U);
@@ -133,7 +133,7 @@ __global__ void k_dt_reduce(CaseK K, DevPtrs<R> P, int by_cells) {
       if (P.phase[p] == 0) continue;
       R sq = P.v[p] * P.v[p];
       for (int k = 1; k < D; k++) sq = sq + P.v[k * K.cap + p] * P.v[k * K.cap + p];
-      R U = rsqrt_<R>(sq);
+      R U = sqrt_r<R>(sq);
       R ds = H[p] / R(CELL_RATIO) * R(CUT_OFF);
       R c12 = amax1(P.c[p], R(0));
       R t = R(K.cfl) * ds / (c12 + U);
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
             sq = (k == 0) ? rv * rv : sq + rv * rv;
           }
           R e_j = P.cE[ss * nc + ci] - R(0.5) * sq / rho;
-          P.cP[ci] = eos_p<R>(e_j, (R)K.gamma[ss], (R)K.pinf[ss]);
+          P.cP[ci] = eos_p<R>(e_j, (R)K.gamma[ss], (R)K.pinf_eos[ss]);
           for (int t = 0; t < U * B; t++) P.ccoef0[(ss * U * B + t) * nc + ci] = P.ccoef[(ss * U * B + t) * nc + ci];
         }
       }
@@ -320,6 +320,11 @@ __global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
         for (int t = 0; t < U * B; t++) {
           P.ccoef[(ss * U * B + t) * nc + ci] = R(0);
           P.ccoef0[(ss * U * B + t) * nc + ci] = R(0);
+        }
+        if (K.eshift[ss] != 0.0) {
+          /* true energy 0, as the reference resets it */
+          P.ccoef[(ss * U * B + (U - 1) * B) * nc + ci] = (R)(-K.eshift[ss]);
+          P.ccoef0[(ss * U * B + (U - 1) * B) * nc + ci] = (R)(-K.eshift[ss]);
         }
         P.crho[ss * nc + ci] = (R)K.ini_rho[ss];
         for (int k = 0; k < D; k++) P.crhov[(ss * D + k) * nc + ci] = R(0);
@@ -415,10 +420,10 @@ __global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
                 sq = (k == 0) ? vj[k] * vj[k] : sq + vj[k] * vj[k];
               }
               R rhoe_j = Ej - R(0.5) * rhoj * sq;
-              R P_j = eos_p<R>(rhoe_j, (R)K.gamma[s1], (R)K.pinf[s1]);
+              R P_j = eos_p<R>(rhoe_j, (R)K.gamma[s1], (R)K.pinf_eos[s1]);
               rhoj = P.crho[s * nc + ci];
               for (int k = 0; k < D; k++) rvj[k] = rhoj * vj[k];
-              Ej = eos_rhoe<R>(P_j, (R)K.gamma[s], (R)K.pinf[s]) + R(0.5) * rhoj * sq;
+              Ej = eos_rhoe<R>(P_j, (R)K.gamma[s], (R)K.pinf_eos[s]) + R(0.5) * rhoj * sq;
             }
             pj[0] += rhoj * aj;
             for (int k = 0; k < D; k++) pj[1 + k] += rvj[k] * aj;
@@ -485,7 +490,7 @@ __global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
     /* positivity probe (mpm.cpp:690-728) */
     const int NPR = (D == 3) ? 8 : 4;
     for (int s = 0; s < F; s++) {
-      const R gs = (R)K.gamma[s], pf = (R)K.pinf[s];
+      const R gs = (R)K.gamma[s], pf = (R)K.pinf[s], pfe = (R)K.pinf_eos[s];
       int fg = 0;
       for (int pr = 0; pr < NPR && !fg; pr++) {
         R Ui[U];
@@ -500,7 +505,7 @@ __global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
         R sq = Ui[1] * Ui[1];
         for (int k = 1; k < D; k++) sq = sq + Ui[1 + k] * Ui[1 + k];
         R e_p = Ui[U - 1] - R(0.5) * sq / Ui[0];
-        R P_p = eos_p<R>(e_p, gs, pf);
+        R P_p = eos_p<R>(e_p, gs, pfe);
         if (P_p < R(-0.05) * pf || Ui[0] < R(0)) fg = 1;
       }
       for (int u = 0; u < U; u++) P.clim[(s * U + u) * nc + ci] = fg ? R(0.) : lim[s][u];
@@ -525,11 +530,12 @@ struct Prim {
 
 /* normal-column flux F[u] = DF[u][a] with DF = U v^T + P I (+ v P in the energy row) */
 template <int D, typename R>
-__device__ __forceinline__ void flux_col(const R* Uu, const R* v, R Pp, int a, R* Fc) {
+__device__ __forceinline__ void flux_col(const R* Uu, const R* v, R Pp, int a, R* Fc, R esh) {
   constexpr int U = D + 2;
   for (int u = 0; u < U; u++) Fc[u] = Uu[u] * v[a];
   Fc[1 + a] += Pp;
   Fc[U - 1] += v[a] * Pp;
+  if (esh != R(0)) Fc[U - 1] += v[a] * esh;   /* (E_true + p) v with E_true = E + esh */
 }
 
 /* MODE 0: MGFM solved inline; MODE 2: queue every interface problem (no flux
@@ -558,7 +564,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
     }
     for (int ss = 0; ss < F; ss++) {
       if (P.cph[ss * nc + ci] != 1) continue;
-      const R gs = (R)K.gamma[ss], pfs = (R)K.pinf[ss];
+      const R gs = (R)K.gamma[ss], pfs = (R)K.pinf[ss], pfe = (R)K.pinf_eos[ss], esh = (R)K.eshift[ss];
       R co[U][B], L[U], dc[U][B];
       for (int u = 0; u < U; u++) {
         for (int b = 0; b < B; b++) {
@@ -583,10 +589,10 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
         R vp[3], sq = Up[1] * Up[1];
         for (int k = 1; k < D; k++) sq = sq + Up[1 + k] * Up[1 + k];
         for (int k = 0; k < D; k++) vp[k] = Up[1 + k] / rho_p;
-        R P_p = eos_p<R>(Up[U - 1] - R(0.5) * sq / rho_p, gs, pfs);
+        R P_p = eos_p<R>(Up[U - 1] - R(0.5) * sq / rho_p, gs, pfe);
         for (int bi = 1; bi <= D; bi++) {
           R Fc[U];
-          flux_col<D, R>(Up, vp, P_p, bi - 1, Fc);
+          flux_col<D, R>(Up, vp, P_p, bi - 1, Fc, esh);
           for (int u = 0; u < U; u++) dc[u][bi] += Fc[u] * gw * voli;
         }
       }
@@ -620,11 +626,11 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
           R v_i[3], sq = Ui[1] * Ui[1];
           for (int k = 1; k < D; k++) sq = sq + Ui[1 + k] * Ui[1 + k];
           for (int k = 0; k < D; k++) v_i[k] = Ui[1 + k] / rho_i;
-          const R P_i = eos_p<R>(E_i - R(0.5) * sq / rho_i, gs, pfs);
-          const R c_i = rsqrt_<R>(gs * (pfs + P_i) / rho_i);
+          const R P_i = eos_p<R>(E_i - R(0.5) * sq / rho_i, gs, pfe);
+          const R c_i = sqrt_r<R>(gs * (pfs + P_i) / rho_i);
           const R vni = v_i[a] * na;
           R Fi[U];
-          flux_col<D, R>(Ui, v_i, P_i, a, Fi);
+          flux_col<D, R>(Ui, v_i, P_i, a, Fi, esh);
           R Nb[B];
           Nb[0] = R(1.);
           for (int d = 0; d < D; d++) Nb[1 + d] = dri[d];
@@ -650,7 +656,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
                 sqj = (k == 0) ? v_j[k] * v_j[k] : sqj + v_j[k] * v_j[k];
               }
               R rhoe_j = E_j - R(0.5) * sqj * rho_j;
-              R P_j = eos_p<R>(rhoe_j, (R)K.gamma[s1], (R)K.pinf[s1]);
+              R P_j = eos_p<R>(rhoe_j, (R)K.gamma[s1], (R)K.pinf_eos[s1]);
               R vnj = v_j[a] * na;
               if (ss != s1) {
                 double gh[3];
@@ -689,15 +695,15 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
                   rhov_j[k] = rho_j * v_j[k];
                   sqj = (k == 0) ? v_j[k] * v_j[k] : sqj + v_j[k] * v_j[k];
                 }
-                E_j = eos_rhoe<R>(P_j, gs, pfs) + R(0.5) * rho_j * sqj;
+                E_j = eos_rhoe<R>(P_j, gs, pfe) + R(0.5) * rho_j * sqj;
               }
-              const R c_j = rsqrt_<R>(gs * (pfs + P_j) / rho_j);
+              const R c_j = sqrt_r<R>(gs * (pfs + P_j) / rho_j);
               R Ujj[U];
               Ujj[0] = rho_j;
               for (int k = 0; k < D; k++) Ujj[1 + k] = rhov_j[k];
               Ujj[U - 1] = E_j;
               R Fj[U];
-              flux_col<D, R>(Ujj, v_j, P_j, a, Fj);
+              flux_col<D, R>(Ujj, v_j, P_j, a, Fj, esh);
               const R vni2 = v_i[a] * na;
               vnj = v_j[a] * na;
               /* HLLC (particle_flow.cpp:232-272) */
@@ -714,6 +720,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
                 UsL[0] = rho_sL;
                 for (int k = 0; k < D; k++) UsL[1 + k] = rho_sL * (v_i[k] + (k == a ? (S_s - vni2) * na : R(0)));
                 UsL[U - 1] = rho_sL * (E_i / rho_i + (S_s - vni2) * (S_s + P_i / (rho_i * (SL - vni2))));
+                if (esh != R(0)) UsL[U - 1] += esh * ((S_s - vni2) / (SL - S_s));   /* esh (rho_star / rho - 1) */
                 for (int u = 0; u < U; u++) Fh[u] = Fi[u] + SL * (UsL[u] - Ui[u]) * na;
               } else if (S_s <= R(0) && SR >= R(0)) {
                 const R rho_sR = rho_j * (SR - vnj) / (SR - S_s);
@@ -721,6 +728,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
                 UsR[0] = rho_sR;
                 for (int k = 0; k < D; k++) UsR[1 + k] = rho_sR * (v_j[k] + (k == a ? (S_s - vnj) * na : R(0)));
                 UsR[U - 1] = rho_sR * (E_j / rho_j + (S_s - vnj) * (S_s + P_j / (rho_j * (SR - vnj))));
+                if (esh != R(0)) UsR[U - 1] += esh * ((S_s - vnj) / (SR - S_s));
                 for (int u = 0; u < U; u++) Fh[u] = Fj[u] + SR * (UsR[u] - Ujj[u]) * na;
               } else if (SR <= R(0)) {
                 for (int u = 0; u < U; u++) Fh[u] = Fj[u];
@@ -749,7 +757,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
                 sqj = (k == 0) ? v_j[k] * v_j[k] : sqj + v_j[k] * v_j[k];
               }
               P_j = (R)K.inlet_p;
-              E_j = eos_rhoe<R>(P_j, gs, pfs) + R(0.5) * sqj * rho_j;
+              E_j = eos_rhoe<R>(P_j, gs, pfe) + R(0.5) * sqj * rho_j;
             }
             if (fc.bound != PGDG_BC_TRANSMISSIVE) {
               if (mirror_j) {
@@ -765,10 +773,10 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
             Uj[0] = rho_j;
             for (int k = 0; k < D; k++) Uj[1 + k] = rhov_j[k];
             Uj[U - 1] = E_j;
-            const R c_j = rsqrt_<R>(gs * (pfs + P_j) / rho_j);
+            const R c_j = sqrt_r<R>(gs * (pfs + P_j) / rho_j);
             const R vnj = v_j[a] * na;
             R Fj[U];
-            flux_col<D, R>(Uj, v_j, P_j, a, Fj);
+            flux_col<D, R>(Uj, v_j, P_j, a, Fj, esh);
             const R SL = amin1(vni - c_i, vnj - c_j);
             const R SR = amax1(vni + c_i, vnj + c_j);
             R Fh[U];
@@ -917,15 +925,15 @@ __global__ void k_update_grid(CaseK K, DevPtrs<R> P, int md) {
         }
         R E = P.ccoef[((s * U + U - 1) * B) * nc + ci];
         P.cE[s * nc + ci] = E;
-        Pc = eos_p<R>(E - R(0.5) * sq / rho, (R)K.gamma[s], (R)K.pinf[s]);
-        c_s = rsqrt_<R>((R)K.gamma[s] * ((R)K.pinf[s] + Pc) / rho);
+        Pc = eos_p<R>(E - R(0.5) * sq / rho, (R)K.gamma[s], (R)K.pinf_eos[s]);
+        c_s = sqrt_r<R>((R)K.gamma[s] * ((R)K.pinf[s] + Pc) / rho);
         R d00 = P.cdcoef[((s * U) * B) * nc + ci];
         R asq = R(0);
         for (int k = 0; k < D; k++) {
           R ak = (P.cdcoef[((s * U + 1 + k) * B) * nc + ci] - d00 * vcur[k]) / rho;
           asq = (k == 0) ? ak * ak : asq + ak * ak;
         }
-        ac_s = rsqrt_<R>(asq);
+        ac_s = sqrt_r<R>(asq);
       }
       P.cc[s * nc + ci] = c_s;
       P.cac[s * nc + ci] = ac_s;
@@ -955,7 +963,9 @@ __global__ void k_totals(CaseK K, DevPtrs<R> P, double* out) {
     if (ph == 0) continue;
     double m = (double)P.rho[p] * (double)P.vol[p];
     acc[ph - 1] += m;
-    acc[2] += (double)P.E[p] * (double)P.vol[p];
+    double e = (double)P.E[p];
+    if (K.eshift[ph - 1] != 0.0) e += K.eshift[ph - 1];
+    acc[2] += e * (double)P.vol[p];
   }
   const int64_t nc = K.ncell;
   double voli = K.ps[0] * K.ps[1] * (D == 3 ? K.ps[2] : 1.0);
@@ -965,7 +975,9 @@ __global__ void k_totals(CaseK K, DevPtrs<R> P, double* out) {
       if (P.cph[s * nc + ci] != 1) continue;
       double a = (double)P.calph[s * nc + ci];
       acc[3 + s] += voli * a * (double)P.crho[s * nc + ci];
-      acc[5] += voli * a * (double)P.cE[s * nc + ci];
+      double e = (double)P.cE[s * nc + ci];
+      if (K.eshift[s] != 0.0) e += K.eshift[s];
+      acc[5] += voli * a * e;
     }
   }
   for (int k = 0; k < 6; k++) {

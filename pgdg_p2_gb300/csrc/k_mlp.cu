@@ -38,11 +38,11 @@ constexpr int NNORM = 2 * NI + 2 * NO;
 /* ------------------------------------------------------------------ */
 /* features of one Riemann problem                                    */
 /* ------------------------------------------------------------------ */
-/* Closed-form baseline of the star pressure: the acoustic estimate
+/* Closed-form baseline p_b of the star pressure: the acoustic estimate
  * p_ac = (Z_r p_l + Z_l p_r + Z_l Z_r (u_l - u_r)) / (Z_l + Z_r), Z = sqrt(gamma (p + p_inf) rho),
  * then one linearised step of the two-shock relation with the shock speeds W
- * (mpm.cpp:908, glbfunc.h:314-337) frozen at max(p_ac, 1e-8).  Returned as an
- * effective pressure p + p_inf_l (> 0). */
+ * (mpm.cpp:908, glbfunc.h:314-337) frozen at max(p_ac, 1e-8).  For weak waves
+ * the error is far below the Newton tolerance; the network corrects strong ones. */
 __host__ __device__ inline double mgfm_baseline(double ul, double ur, double pl, double pr, double rl, double rr,
                                                 double gl, double il, double gr, double ir) {
   const double Zl = sqrt(gl * (pl + il) * rl), Zr = sqrt(gr * (pr + ir) * rr);
@@ -52,50 +52,57 @@ __host__ __device__ inline double mgfm_baseline(double ul, double ur, double pl,
   const double Wr = sqrt(0.5 * rr * ((gr + 1.) * p0 + (gr - 1.) * pr + 2. * gr * ir));
   double pt = (pl / Wl + pr / Wr + (ul - ur)) / (1. / Wl + 1. / Wr);
   if (!(pt > 1e-8)) pt = 1e-8;
-  return pt + il;
+  return pt;
 }
 
-/* Scale-free description: effective pressures p + p_inf relative to the larger
- * one, density ratio, velocity jump in units of sqrt(P0/rho0), the two gammas,
- * the stiffness fractions, the raw pressures and the closed-form baseline, all
- * relative to P0.  The network's first output is log((p* + p_inf_l) / Pb). */
-__host__ __device__ inline void mgfm_features(const double* q, double gl, double pl_inf, double gr, double pr_inf,
-                                              float* x, double* P0_out, double* a0_out, double* Pb_out) {
+/* Scale-free description of a problem (FP32 transcendentals; the baseline in
+ * FP64):
+ *   x0,x1  log((p + p_inf)/P0) left/right, P0 the larger effective pressure
+ *   x2     log(rho_l / rho_r)
+ *   x3     (u_l - u_r) / a0, a0 = sqrt(P0 / sqrt(rho_l rho_r)), clamped to +-20
+ *   x4     log(p_b / p_l)          x11  log(p_b / p_r)
+ *   x5,x6  gamma left/right        x7,x8  p_inf / P0 left/right
+ *   x9,x10 log(p / P0) left/right
+ * The network's first output y predicts log(p* / p_b) / sc with the strength
+ * scale sc = s^2 / (1 + s^2), s = |x4| + |x11|: the correction vanishes for
+ * weak waves, where the baseline is already far inside the Newton tolerance. */
+__host__ __device__ inline void mgfm_features(const double* q, double gl, double il, double gr, double ir, float* x,
+                                              double* pb_out, float* sc_out) {
   double ul = q[0], ur = q[1], pl = q[2], pr = q[3], rl = q[4], rr = q[5];
   if (pl < 1e-10) pl = 1e-10;
   if (pr < 1e-10) pr = 1e-10;
   if (rl < 1e-10) rl = 1e-10;
   if (rr < 1e-10) rr = 1e-10;
-  double Pl = pl + pl_inf, Pr = pr + pr_inf;
-  double P0 = Pl > Pr ? Pl : Pr;
-  double r0 = sqrt(rl * rr);
-  double a0 = sqrt(P0 / r0);
-  double du = (ul - ur) / a0;
-  double Pb = mgfm_baseline(ul, ur, pl, pr, rl, rr, gl, pl_inf, gr, pr_inf);
-  x[0] = (float)log(Pl / P0);
-  x[1] = (float)log(Pr / P0);
-  x[2] = (float)log(rl / rr);
-  x[3] = (float)(du > 20 ? 20 : (du < -20 ? -20 : du));
-  x[4] = (float)asinh(du);
+  const double Pl = pl + il, Pr = pr + ir;
+  const double P0 = Pl > Pr ? Pl : Pr;
+  const float a0 = sqrtf((float)P0 / sqrtf((float)rl * (float)rr));
+  const float du = (float)(ul - ur) / a0;
+  const double pb = mgfm_baseline(ul, ur, pl, pr, rl, rr, gl, il, gr, ir);
+  const float lbl = logf((float)(pb / pl)), lbr = logf((float)(pb / pr));
+  const float sv = fabsf(lbl) + fabsf(lbr);
+  x[0] = logf((float)(Pl / P0));
+  x[1] = logf((float)(Pr / P0));
+  x[2] = logf((float)(rl / rr));
+  x[3] = du > 20.f ? 20.f : (du < -20.f ? -20.f : du);
+  x[4] = lbl;
   x[5] = (float)gl;
   x[6] = (float)gr;
-  x[7] = (float)(pl_inf / P0);
-  x[8] = (float)(pr_inf / P0);
-  x[9] = (float)log(pl / P0 + 1e-30);
-  x[10] = (float)log(pr / P0 + 1e-30);
-  x[11] = (float)log(Pb / P0);
-  *P0_out = P0;
-  *a0_out = a0;
-  *Pb_out = Pb;
+  x[7] = (float)(il / P0);
+  x[8] = (float)(ir / P0);
+  x[9] = logf((float)(pl / P0 + 1e-30));
+  x[10] = logf((float)(pr / P0 + 1e-30));
+  x[11] = lbr;
+  *pb_out = pb;
+  *sc_out = sv * sv / (1.f + sv * sv);
 }
 
 __global__ void k_features(const double* in6, const int8_t* mat2, const double* gam, const double* pinf, float* X,
                            int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     int s = mat2[2 * i], s1 = mat2[2 * i + 1];
-    double P0, a0, Pb;
-    float x[NI];
-    mgfm_features(in6 + 6 * i, gam[s], pinf[s], gam[s1], pinf[s1], x, &P0, &a0, &Pb);
+    double pb;
+    float sc, x[NI];
+    mgfm_features(in6 + 6 * i, gam[s], pinf[s], gam[s1], pinf[s1], x, &pb, &sc);
     for (int k = 0; k < NI; k++) X[i * NI + k] = x[k];
   }
 }
@@ -109,61 +116,80 @@ __device__ __forceinline__ float wq(float w) {
   return w;
 }
 
-/* Y[n][2] (normalised outputs); optionally store hidden activations for the
- * backward pass (A1,A2,A3 [n][64]) */
+/* stage the parameters in shared memory, weights rounded to BF16 when asked */
 template <bool BF16>
-__global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ params, const float* __restrict__ X,
-                                                     float* __restrict__ Y, float* A1, float* A2, float* A3,
-                                                     int64_t n, int xnorm) {
-  __shared__ float w[NPARAM + NNORM];
+__device__ __forceinline__ void load_params(const float* __restrict__ params, float* w) {
   for (int k = threadIdx.x; k < NPARAM; k += blockDim.x) {
     bool isb = (k >= OFF_B1 && k < OFF_W2) || (k >= OFF_B2 && k < OFF_W3) || (k >= OFF_B3 && k < OFF_W4) || k >= OFF_B4;
     w[k] = isb ? params[k] : wq<BF16>(params[k]);
   }
   for (int k = threadIdx.x; k < NNORM; k += blockDim.x) w[NPARAM + k] = params[NPARAM + k];
   __syncthreads();
+}
+
+/* one sample through the network (normalised input xn); the loops are fully
+ * unrolled so the activations stay in registers; A1..A3 (optional) receive the
+ * hidden activations for the backward pass */
+template <int NOUT>
+__device__ __forceinline__ void mlp_eval(const float* w, const float* xn, float* y, float* A1, float* A2, float* A3,
+                                         int64_t i) {
+  float h[NH], g[NH];
+#pragma unroll
+  for (int j = 0; j < NH; j++) {
+    float a = w[OFF_B1 + j];
+#pragma unroll
+    for (int k = 0; k < NI; k++) a = fmaf(w[OFF_W1 + j * NI + k], xn[k], a);
+    h[j] = tanhf(a);
+  }
+  if (A1)
+#pragma unroll
+    for (int j = 0; j < NH; j++) A1[i * NH + j] = h[j];
+#pragma unroll
+  for (int j = 0; j < NH; j++) {
+    float a = w[OFF_B2 + j];
+#pragma unroll
+    for (int k = 0; k < NH; k++) a = fmaf(w[OFF_W2 + j * NH + k], h[k], a);
+    g[j] = tanhf(a);
+  }
+  if (A2)
+#pragma unroll
+    for (int j = 0; j < NH; j++) A2[i * NH + j] = g[j];
+#pragma unroll
+  for (int j = 0; j < NH; j++) {
+    float a = w[OFF_B3 + j];
+#pragma unroll
+    for (int k = 0; k < NH; k++) a = fmaf(w[OFF_W3 + j * NH + k], g[k], a);
+    h[j] = tanhf(a);
+  }
+  if (A3)
+#pragma unroll
+    for (int j = 0; j < NH; j++) A3[i * NH + j] = h[j];
+#pragma unroll
+  for (int o = 0; o < NOUT; o++) {
+    float a = w[OFF_B4 + o];
+#pragma unroll
+    for (int k = 0; k < NH; k++) a = fmaf(w[OFF_W4 + o * NH + k], h[k], a);
+    y[o] = a;
+  }
+}
+
+/* Y[n][2] (normalised outputs) from raw features X; optionally store hidden
+ * activations for the backward pass (A1,A2,A3 [n][64]) */
+template <bool BF16>
+__global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ params, const float* __restrict__ X,
+                                                     float* __restrict__ Y, float* A1, float* A2, float* A3,
+                                                     int64_t n) {
+  __shared__ __align__(16) float w[NPARAM + NNORM];
+  load_params<BF16>(params, w);
   const float* mx = w + NPARAM;
   const float* sx = mx + NI;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    float x[NI];
-    for (int k = 0; k < NI; k++) {
-      float v = X[i * NI + k];
-      x[k] = xnorm ? (v - mx[k]) / sx[k] : v;
-    }
-    float h[NH], g[NH];
-#pragma unroll 8
-    for (int j = 0; j < NH; j++) {
-      float a = w[OFF_B1 + j];
+    float xn[NI], y[NO];
 #pragma unroll
-      for (int k = 0; k < NI; k++) a = fmaf(w[OFF_W1 + j * NI + k], x[k], a);
-      h[j] = tanhf(a);
-    }
-    if (A1)
-      for (int j = 0; j < NH; j++) A1[i * NH + j] = h[j];
-#pragma unroll 4
-    for (int j = 0; j < NH; j++) {
-      float a = w[OFF_B2 + j];
-#pragma unroll
-      for (int k = 0; k < NH; k++) a = fmaf(w[OFF_W2 + j * NH + k], h[k], a);
-      g[j] = tanhf(a);
-    }
-    if (A2)
-      for (int j = 0; j < NH; j++) A2[i * NH + j] = g[j];
-#pragma unroll 4
-    for (int j = 0; j < NH; j++) {
-      float a = w[OFF_B3 + j];
-#pragma unroll
-      for (int k = 0; k < NH; k++) a = fmaf(w[OFF_W3 + j * NH + k], g[k], a);
-      h[j] = tanhf(a);
-    }
-    if (A3)
-      for (int j = 0; j < NH; j++) A3[i * NH + j] = h[j];
-    for (int o = 0; o < NO; o++) {
-      float a = w[OFF_B4 + o];
-#pragma unroll
-      for (int k = 0; k < NH; k++) a = fmaf(w[OFF_W4 + o * NH + k], h[k], a);
-      Y[i * NO + o] = a;
-    }
+    for (int k = 0; k < NI; k++) xn[k] = (X[i * NI + k] - mx[k]) / sx[k];
+    mlp_eval<NO>(w, xn, y, A1, A2, A3, i);
+    Y[i * NO + 0] = y[0];
+    Y[i * NO + 1] = y[1];
   }
 }
 
@@ -255,43 +281,62 @@ __device__ __forceinline__ double mgfm_f(double ul, double ur, double pl, double
   return ul - ur - (p - pl) / Wl - (p - pr) / Wr;
 }
 
-/* seed from the network output (normalised targets), or -1 when the problem has
- * no positive root and must take the plain path */
-__device__ __forceinline__ double seed_from(const double* q, double gl, double pinfl, double gr, double pinfr,
-                                            int variant, float y0, const float* params) {
-  double ul = q[0], ur = q[1], pl = q[2], pr = q[3], rl = q[4], rr = q[5];
-  if (variant == 0) {
-    pl = amax1(pl, 1e-10);
-    pr = amax1(pr, 1e-10);
-    rl = amax1(rl, 1e-10);
-    rr = amax1(rr, 1e-10);
-  } else {
-    if (pl < 0) pl = 0;
-    if (pr < 0) pr = 0;
+/* Seeds of a batch: features, network and seed p_b exp(sc y) in one pass per
+ * problem; -1 (plain solve) for a problem without a positive root, f(1e-8) < 0,
+ * evaluated with the clamps of the MGFM variant (mpm.cpp:886-893). */
+template <bool BF16>
+__global__ void __launch_bounds__(128) k_seed(const float* __restrict__ params, const double* __restrict__ in6,
+                                              const int8_t* __restrict__ mat2, const double* __restrict__ gam,
+                                              const double* __restrict__ pinf, int variant, double* __restrict__ seed,
+                                              int64_t n) {
+  __shared__ __align__(16) float w[NPARAM + NNORM];
+  load_params<BF16>(params, w);
+  const float* mx = w + NPARAM;
+  const float* sx = mx + NI;
+  const float my0 = w[NPARAM + 2 * NI], sy0 = w[NPARAM + 2 * NI + NO];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double* q = in6 + 6 * i;
+    const int s = mat2[2 * i], s1 = mat2[2 * i + 1];
+    const double gl = gam[s], il = pinf[s], gr = gam[s1], ir = pinf[s1];
+    double pl = q[2], pr = q[3], rl = q[4], rr = q[5];
+    if (variant == 0) {
+      pl = amax1(pl, 1e-10);
+      pr = amax1(pr, 1e-10);
+      rl = amax1(rl, 1e-10);
+      rr = amax1(rr, 1e-10);
+    } else {
+      if (pl < 0) pl = 0;
+      if (pr < 0) pr = 0;
+    }
+    if (mgfm_f(q[0], q[1], pl, pr, rl, rr, gl, il, gr, ir, 1e-8) < 0) {
+      seed[i] = -1.0;
+      continue;
+    }
+    double pb;
+    float sc, xn[NI], y[1];
+    mgfm_features(q, gl, il, gr, ir, xn, &pb, &sc);
+#pragma unroll
+    for (int k = 0; k < NI; k++) xn[k] = (xn[k] - mx[k]) / sx[k];
+    mlp_eval<1>(w, xn, y, nullptr, nullptr, nullptr, i);
+    double ps = pb * (double)expf(sc * (y[0] * sy0 + my0));
+    seed[i] = ps > 1e-8 ? ps : 1e-8;
   }
-  if (mgfm_f(ul, ur, pl, pr, rl, rr, gl, pinfl, gr, pinfr, 1e-8) < 0) return -1.0;
-  const float* my = params + NPARAM + 2 * NI;
-  const float* sy = my + NO;
-  double P0, a0, Pb;
-  float x[NI];
-  mgfm_features(q, gl, pinfl, gr, pinfr, x, &P0, &a0, &Pb);
-  double lp = (double)(y0 * sy[0] + my[0]);  /* log((p* + p_inf_l) / Pb) */
-  double ps = exp(lp) * Pb - pinfl;
-  if (!(ps > 1e-8)) ps = 1e-8;
-  return ps;
 }
 
+/* Newton from the seed (or the plain seed when seed is NULL or the entry is
+ * negative); a seeded solve that has not converged at the cap is redone from
+ * the plain seed, and its iterations are counted together */
 __global__ void k_mgfm_seeded(const double* __restrict__ in6, const int8_t* __restrict__ mat2,
                               const double* __restrict__ gam, const double* __restrict__ pinf, int variant,
-                              const float* __restrict__ Y, const float* __restrict__ params, double* __restrict__ out3,
-                              int32_t* __restrict__ iters, int64_t n, unsigned long long* stats) {
+                              const double* __restrict__ seed, double* __restrict__ out3, int32_t* __restrict__ iters,
+                              int64_t n, unsigned long long* stats) {
   unsigned long long nit = 0, nmax = 0, ncall = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double* q = in6 + 6 * i;
     int s = mat2[2 * i], s1 = mat2[2 * i + 1];
     double o[3];
     int it = 0;
-    double sd = Y ? seed_from(q, gam[s], pinf[s], gam[s1], pinf[s1], variant, Y[i * NO], params) : -1.0;
+    const double sd = seed ? seed[i] : -1.0;
     bool done = false;
     if (sd > 0) {
       it = mgfm(q[0], q[1], q[2], q[3], q[4], q[5], gam[s], pinf[s], gam[s1], pinf[s1], variant, sd, o);
@@ -330,6 +375,17 @@ struct pgdg_mlp {
         *dZ3 = nullptr, *dZ2 = nullptr, *dZ1 = nullptr;
   double* d_loss = nullptr;
   int64_t cap = 0;
+  double* seeds = nullptr; /* per-problem seeds of batched solves */
+  int64_t seeds_cap = 0;
+  int reserve_seeds(int64_t n) {
+    if (n <= seeds_cap) return PGDG_OK;
+    if (seeds) cudaFree(seeds);
+    seeds = nullptr;
+    seeds_cap = 0;
+    if (cudaMalloc((void**)&seeds, sizeof(double) * n) != cudaSuccess) return PGDG_ENOMEM;
+    seeds_cap = n;
+    return PGDG_OK;
+  }
   int reserve(int64_t n) {
     if (n <= cap) return PGDG_OK;
     float** bufs[] = {&X, &Xn, &Y, &A1, &A2, &A3, &dZ4, &dZ3, &dZ2, &dZ1};
@@ -346,6 +402,7 @@ struct pgdg_mlp {
     for (float* b : bufs)
       if (b) cudaFree(b);
     if (d_loss) cudaFree(d_loss);
+    if (seeds) cudaFree(seeds);
   }
 };
 
@@ -356,8 +413,13 @@ inline int g_for(int64_t n, int b) {
   return g < 1 ? 1 : (int)g;
 }
 void forward(pgdg_mlp* m, const float* X, float* Y, float* A1, float* A2, float* A3, int64_t n, cudaStream_t st) {
-  if (m->bf16) k_mlp_forward<true><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n, 1);
-  else k_mlp_forward<false><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n, 1);
+  if (m->bf16) k_mlp_forward<true><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n);
+  else k_mlp_forward<false><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n);
+}
+void seed_launch(pgdg_mlp* m, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
+                 int variant, double* seed, int64_t n, cudaStream_t st) {
+  if (m->bf16) k_seed<true><<<g_for(n, 128), 128, 0, st>>>(m->d_params, in6, mat2, gam, pinf, variant, seed, n);
+  else k_seed<false><<<g_for(n, 128), 128, 0, st>>>(m->d_params, in6, mat2, gam, pinf, variant, seed, n);
 }
 /* gradient of the mean squared error of the normalised outputs into m->d_g */
 void gradients(pgdg_mlp* m, const float* X, const float* T, int64_t n, cudaStream_t st) {
@@ -467,37 +529,25 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
                       const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n) {
   if (n < 0 || !in6 || !mat2 || !gam || !pinf || !out3 || nmat < 1) return PGDG_EINVAL;
   if (n == 0) return PGDG_OK;
-  pgdg_mlp* m = const_cast<pgdg_mlp*>(net);
-  const float* Y = nullptr;
-  if (m) {
-    int rc = m->reserve(n);
-    if (rc) return rc;
-    k_features<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, m->X, n);
-    forward(m, m->X, m->Y, nullptr, nullptr, nullptr, n, 0);
-    Y = m->Y;
-  }
-  k_mgfm_seeded<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, variant, Y, m ? m->d_params : nullptr, out3, iters, n,
-                                        nullptr);
-  return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
+  return mgfm_seeded_run((void*)net, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr, 0);
 }
 
 }  // extern "C"
 
 namespace pgdg {
 int mgfm_seeded_run(void* netv, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
-                    int variant, double* out3, int64_t n, unsigned long long* stats, cudaStream_t st) {
+                    int variant, double* out3, int32_t* iters, int64_t n, unsigned long long* stats,
+                    cudaStream_t st) {
   if (n <= 0) return PGDG_OK;
   pgdg_mlp* m = static_cast<pgdg_mlp*>(netv);
-  const float* Y = nullptr;
+  const double* sd = nullptr;
   if (m) {
-    int rc = m->reserve(n);
+    int rc = m->reserve_seeds(n);
     if (rc) return rc;
-    k_features<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, m->X, n);
-    forward(m, m->X, m->Y, nullptr, nullptr, nullptr, n, st);
-    Y = m->Y;
+    seed_launch(m, in6, mat2, gam, pinf, variant, m->seeds, n, st);
+    sd = m->seeds;
   }
-  k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, Y, m ? m->d_params : nullptr, out3,
-                                               nullptr, n, stats);
+  k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, stats);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 }  // namespace pgdg

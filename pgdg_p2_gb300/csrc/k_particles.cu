@@ -304,7 +304,7 @@ __device__ void eos_fill(const CaseK& K, PState<D>& s) {
   int ph = s.phase - 1;
   double g = K.gamma[ph], pf = K.pinf[ph];
   double ei = dsub(s.E, dmul(dmul(0.5, s.rho), sqnorm<D>(s.v)));
-  s.P = eos_p_x(ei, g, pf);
+  s.P = eos_p_x(ei, g, K.pinf_eos[ph]);
   s.c = dsqrt(ddiv(dmul(g, dadd(pf, s.P)), s.rho));
 }
 

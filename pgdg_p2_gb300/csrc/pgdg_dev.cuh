@@ -69,6 +69,11 @@ struct CaseK {
   double bl[3], br[3], ps[3];
   double p_g, p_sz;
   double gamma[F], pinf[F], ini_rho[F];
+  /* energy shift of the FP32 path: stored E = E_true - eshift[s] with
+   * eshift = gamma p_inf / (gamma - 1), so the EOS reads p = (gamma-1)(E - rho v^2/2)
+   * without the cancellation against gamma p_inf (pinf_eos = 0); both are 0 and
+   * pinf on the FP64 paths, which store E unshifted */
+  double eshift[F], pinf_eos[F];
   double inlet_rho, inlet_u[3], inlet_p;
   double cfl;
   double vol_max, vol_min, dss0;
@@ -210,7 +215,8 @@ struct Launch {
 /* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls, iterations, cap hits) */
 struct pgdg_mlp_fwd;
 int mgfm_seeded_run(void* net, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
-                    int variant, double* out3, int64_t n, unsigned long long* stats, cudaStream_t st);
+                    int variant, double* out3, int32_t* iters, int64_t n, unsigned long long* stats,
+                    cudaStream_t st);
 
 /* shared helpers used by several translation units */
 int grid_for(int64_t n, int block);

@@ -97,11 +97,11 @@ template <typename R>
 PGDG_HD R eos_rhoe(R p, R g, R pinf) { return (p + g * pinf) / (g - R(1)); }
 
 template <typename R>
-PGDG_HD R rsqrt_(R x);
+PGDG_HD R sqrt_r(R x);
 template <>
-PGDG_HD double rsqrt_<double>(double x) { return sqrt(x); }
+PGDG_HD double sqrt_r<double>(double x) { return sqrt(x); }
 template <>
-PGDG_HD float rsqrt_<float>(float x) { return sqrtf(x); }
+PGDG_HD float sqrt_r<float>(float x) { return sqrtf(x); }
 
 /* Wendland C4 normalisation C(h) (particle.cpp:139-141) */
 template <typename R>

@@ -2,8 +2,9 @@
 
 The network (csrc/k_mlp.cu) predicts, from 12 scale-free features of a
 two-material Riemann problem, the star pressure as a log correction to a
-closed-form two-shock baseline Pb (log((p* + p_inf_l)/Pb)) and the star velocity
-(as (u* - (u_l+u_r)/2)/a0, trained with weight 1/100: it does not seed Newton).  Training targets are exact roots
+closed-form two-shock baseline p_b, scaled by the wave strength
+(log(p*/p_b)/sc, sc = s^2/(1+s^2)), and the star velocity (as
+(u* - (u_l+u_r)/2)/a0, trained with weight 1/100: it does not seed Newton).  Training targets are exact roots
 of the two-shock relation of MPM::MGFM (mpm.cpp:882-926,
 glbfunc.h:314-337) found by bisection in FP64; problems without a positive root
 (cavitating) are excluded -- the solver sends those straight to the plain solve.
@@ -99,39 +100,52 @@ def exact_roots(in6, mat, gam, pinf, variant=0):
 
 def baseline_np(ul, ur, pl, pr, rl, rr, gl, il, gr, ir):
     """Closed-form star-pressure baseline of the device (mgfm_baseline): the
-    acoustic estimate, then one linearised two-shock step; returns p + p_inf_l."""
+    acoustic estimate, then one linearised two-shock step (a pressure, >= 1e-8)."""
     Zl, Zr = np.sqrt(gl * (pl + il) * rl), np.sqrt(gr * (pr + ir) * rr)
     p0 = (Zr * pl + Zl * pr + Zl * Zr * (ul - ur)) / (Zl + Zr)
     p0 = np.where(p0 > 1e-8, p0, 1e-8)
     Wl = np.sqrt(0.5 * rl * ((gl + 1.) * p0 + (gl - 1.) * pl + 2. * gl * il))
     Wr = np.sqrt(0.5 * rr * ((gr + 1.) * p0 + (gr - 1.) * pr + 2. * gr * ir))
     pt = (pl / Wl + pr / Wr + (ul - ur)) / (1. / Wl + 1. / Wr)
-    pt = np.where(pt > 1e-8, pt, 1e-8)
-    return pt + il
+    return np.where(pt > 1e-8, pt, 1e-8)
 
 
 def features_np(in6, mat, gam, pinf):
-    """Host restatement of the device feature map; returns (X, P0, a0, Pb)."""
+    """Host restatement of the device feature map (mgfm_features); returns
+    (X [n,12] float32, p_b, sc) with the correction scale sc = s^2/(1+s^2)."""
+    f32 = np.float32
     ul, ur, pl, pr, rl, rr = (in6[:, k].astype(np.float64) for k in range(6))
     pl, pr, rl, rr = (np.maximum(x, 1e-10) for x in (pl, pr, rl, rr))
     gl, gr = gam[mat[:, 0]], gam[mat[:, 1]]
     il, ir = pinf[mat[:, 0]], pinf[mat[:, 1]]
     Pl, Pr = pl + il, pr + ir
     P0 = np.maximum(Pl, Pr)
-    r0 = np.sqrt(rl * rr)
-    a0 = np.sqrt(P0 / r0)
-    du = (ul - ur) / a0
-    Pb = baseline_np(ul, ur, pl, pr, rl, rr, gl, il, gr, ir)
-    X = np.stack([np.log(Pl / P0), np.log(Pr / P0), np.log(rl / rr), np.clip(du, -20, 20), np.arcsinh(du), gl, gr,
-                  il / P0, ir / P0, np.log(pl / P0 + 1e-30), np.log(pr / P0 + 1e-30), np.log(Pb / P0)], 1)
-    return X.astype(np.float32), P0, a0, Pb
+    a0 = np.sqrt(P0.astype(f32) / np.sqrt(rl.astype(f32) * rr.astype(f32)))
+    du = (ul - ur).astype(f32) / a0
+    pb = baseline_np(ul, ur, pl, pr, rl, rr, gl, il, gr, ir)
+    lbl = np.log((pb / pl).astype(f32))
+    lbr = np.log((pb / pr).astype(f32))
+    sv = np.abs(lbl) + np.abs(lbr)
+    X = np.stack([np.log((Pl / P0).astype(f32)), np.log((Pr / P0).astype(f32)), np.log((rl / rr).astype(f32)),
+                  np.clip(du, f32(-20), f32(20)), lbl, gl.astype(f32), gr.astype(f32), (il / P0).astype(f32),
+                  (ir / P0).astype(f32), np.log((pl / P0 + 1e-30).astype(f32)), np.log((pr / P0 + 1e-30).astype(f32)),
+                  lbr], 1)
+    return X.astype(f32), pb, (sv * sv / (f32(1) + sv * sv)).astype(f32)
 
 
 def targets_np(in6, mat, gam, pinf, ps, us):
+    """Network targets: log(p*/p_b)/sc (0 where sc < 1e-6, clipped to +-6) and
+    (u* - (u_l+u_r)/2)/a0."""
     ul, ur = in6[:, 0], in6[:, 1]
-    il = pinf[mat[:, 0]]
-    _, P0, a0, Pb = features_np(in6, mat, gam, pinf)
-    return np.stack([np.log((ps + il) / Pb), (us - 0.5 * (ul + ur)) / a0], 1).astype(np.float32)
+    rl, rr = np.maximum(in6[:, 4], 1e-10), np.maximum(in6[:, 5], 1e-10)
+    il, ir = pinf[mat[:, 0]], pinf[mat[:, 1]]
+    P0 = np.maximum(np.maximum(in6[:, 2], 1e-10) + il, np.maximum(in6[:, 3], 1e-10) + ir)
+    a0 = np.sqrt(P0 / np.sqrt(rl * rr))
+    _, pb, sc = features_np(in6, mat, gam, pinf)
+    sc = sc.astype(np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        y0 = np.where(sc > 1e-6, np.log(ps / pb) / sc, 0.0)
+    return np.stack([np.clip(y0, -6, 6), (us - 0.5 * (ul + ur)) / a0], 1).astype(np.float32)
 
 
 def baseline_params():

@@ -85,7 +85,7 @@ def main(argv=None):
     Xs, Ts = [], []
     for in6, mat, gam, pinf in ((sin6, smat, sgam, spinf), (cin6, cmat, S.C5_GAMMA, S.C5_PINF)):
         ps, us, has = S.exact_roots(in6, mat, gam, pinf)
-        X, _, _, _ = S.features_np(in6[has], mat[has], gam, pinf)
+        X, _, _ = S.features_np(in6[has], mat[has], gam, pinf)
         T = S.targets_np(in6[has], mat[has], gam, pinf, ps[has], us[has])
         ok = np.all(np.isfinite(X), 1) & np.all(np.isfinite(T), 1)
         Xs.append(X[ok])

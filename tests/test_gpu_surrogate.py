@@ -21,7 +21,7 @@ def _c5(n, seed):
     from pgdg_p2_gb300 import surrogate as S
     in6, mat = S.c5_problems(n, seed=seed)
     ps, us, has = S.exact_roots(in6, mat, S.C5_GAMMA, S.C5_PINF)
-    X, _, _, _ = S.features_np(in6, mat, S.C5_GAMMA, S.C5_PINF)
+    X, _, _ = S.features_np(in6, mat, S.C5_GAMMA, S.C5_PINF)
     T = S.targets_np(in6, mat, S.C5_GAMMA, S.C5_PINF, ps, us)
     return in6, mat, X[has], T[has], has
 
@@ -36,7 +36,7 @@ def test_features_match_host(gpu_mod):
     torch.cuda.synchronize()
     assert gpu_mod.lib().pgdg_surrogate_features(*[a.data_ptr() for a in args], X.data_ptr(), len(in6)) == 0
     torch.cuda.synchronize()
-    Xh, _, _, _ = S.features_np(in6, mat, S.C5_GAMMA, S.C5_PINF)
+    Xh, _, _ = S.features_np(in6, mat, S.C5_GAMMA, S.C5_PINF)
     np.testing.assert_allclose(X.cpu().numpy(), Xh, rtol=1e-6, atol=1e-6)
 
 
@@ -91,17 +91,31 @@ def test_training_reduces_loss(gpu_mod):
     assert hist[-1][1] < 0.5 * hist[0][1], hist
 
 
+def _residual(in6, mat, gam, pinf, p):
+    """|f(p)| of the two-shock relation (mpm.cpp:908) with the 3D clamps."""
+    from pgdg_p2_gb300 import surrogate as S
+    ul, ur = in6[:, 0], in6[:, 1]
+    pl, pr, rl, rr = (np.maximum(in6[:, k], 1e-10) for k in (2, 3, 4, 5))
+    gl, gr = gam[mat[:, 0]], gam[mat[:, 1]]
+    il, ir = pinf[mat[:, 0]], pinf[mat[:, 1]]
+    return np.abs(ul - ur - (p - pl) / S._W(rl, pl, p, gl, il) - (p - pr) / S._W(rr, pr, p, gr, ir))
+
+
 def _check_seeded(in6, mat, gam, pinf, net, variant=0):
+    """The seeded solve meets the plain solve's own convergence test: |f| <= tol
+    at its p*, u* within 2 tol of the plain u*, p* equal to 1e-4 for 99% of the
+    problems (where f is flat within tol, p* is only fixed to within that band,
+    for either seed); problems without a root take the plain path bit for bit."""
     from pgdg_p2_gb300 import surrogate as S
     op, ip = S.mgfm_gpu(in6, mat, gam, pinf, None, variant)
     osd, isd = S.mgfm_gpu(in6, mat, gam, pinf, net, variant)
     conv = ip < 50
     tol = np.maximum(1e-8, 1e-3 * np.abs(in6[:, 0] - in6[:, 1]))
-    # both solves stop within the Newton tolerance of the same root
+    assert np.all(isd[conv] < 100)
+    assert np.all(_residual(in6[conv], mat[conv], gam, pinf, osd[conv, 1]) <= tol[conv] * (1 + 1e-9))
     assert np.all(np.abs(osd[conv, 2] - op[conv, 2]) <= 2 * tol[conv])
     rel = np.abs(osd[conv, 1] - op[conv, 1]) / op[conv, 1]
-    assert rel.max() <= 5e-3 and np.quantile(rel, 0.99) <= 1e-4
-    # problems without a root take the plain path unchanged
+    assert np.quantile(rel, 0.99) <= 1e-4
     assert osd[~conv].tobytes() == op[~conv].tobytes()
     return ip, isd, conv
 
@@ -115,15 +129,23 @@ def test_seeded_solve_untrained_falls_back(gpu_mod):
 
 
 def test_seeded_solve_trained_saves_iterations(gpu_mod):
+    """What the trained network gains: Newton iterations on the problems with a
+    root against the plain seed (at least 40% fewer) and against its own
+    closed-form baseline used alone (fewer)."""
     from pgdg_p2_gb300 import surrogate as S
     p = S.load_default()
     assert p is not None, "trained weights missing"
     in6, mat = S.c5_problems(1 << 16, seed=5)
     net = S.Surrogate(p)
+    base = S.Surrogate(S.baseline_params())
     ip, isd, conv = _check_seeded(in6, mat, S.C5_GAMMA, S.C5_PINF, net)
-    # Newton iterations on the problems with a root: at least 30% fewer
-    assert isd[conv].mean() <= 0.7 * ip[conv].mean(), (isd[conv].mean(), ip[conv].mean())
+    _, ib, _ = _check_seeded(in6, mat, S.C5_GAMMA, S.C5_PINF, base)
+    print("C5 rooted mean iterations: plain %.3f baseline %.3f learned %.3f"
+          % (ip[conv].mean(), ib[conv].mean(), isd[conv].mean()))
+    assert isd[conv].mean() <= 0.6 * ip[conv].mean()
+    assert isd[conv].mean() < ib[conv].mean()
     net.close()
+    base.close()
 
 
 @pytest.mark.parametrize("cid,grid,steps", [(3, (96, 24, 24), 10), (4, (128, 128), 10)])
@@ -160,6 +182,14 @@ def test_queued_residual_vs_oracle(gpu_mod, oracle_mod, cid, grid, steps):
         assert set(np.unique(mat)) <= {0, 1}
     g.sync()
     assert nq > 0
+    if net is not None and len(in6):
+        # the solver's own last-stage problems: the seeded solve meets the same bar
+        gam, pinf = np.array(cs.gamma[:2]), np.array(cs.pinf[:2])
+        ip, isd, conv = _check_seeded(in6, mat, gam, pinf, net, cs.mgfm_variant)
+        assert isd.mean() <= ip.mean() + 0.05, (isd.mean(), ip.mean())
     per, mom = conserved_l1(cs, g.download_cells(), o.download_cells())
+    # with the learned seed the Newton solve stops elsewhere inside its own
+    # tolerance band |f| <= 1e-3 |u_l - u_r| than the oracle's plain solve; in
+    # stiff water that band is worth about 1e-3 of the momentum
     tol = 1e-3 if cid != 4 else 2e-3
     assert per[0] <= tol and per[-1] <= tol and max(mom) <= tol, (per, mom)

@@ -128,6 +128,24 @@ int pgdg_iface_download(pgdg_ctx* ctx, double* in6, int8_t* mat2, int64_t cap, i
 int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2, const double* gam,
                       const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n);
 
+/* ---- batched MGFM that allocates nothing (no counterpart in the reference) ----
+ * The same solve and results as pgdg_mgfm_batched, for callers that cannot
+ * allocate device memory: a host driver whose own pool already holds the free
+ * device memory (cudaMalloc would fail there), and per-stage callers that
+ * cannot absorb the device-wide synchronisation of cudaFree (the allocating
+ * entry point frees and regrows its seed buffer when a batch outgrows it).
+ * The per-problem seeds live in a fixed device array of
+ * PGDG_MGFM_NOALLOC_MAX entries (8 MiB); a larger n returns PGDG_EOVERFLOW
+ * before anything is launched.  Nothing in that array is read before it is
+ * written, so nothing is cleared.  The first call on a device looks the array
+ * up (cudaGetSymbolAddress) and should come before any stream capture.
+ * Overlapping calls on one device (several host threads, or per-thread default
+ * streams) share the array and race: serialise them.  Device pointers; the
+ * default stream. */
+#define PGDG_MGFM_NOALLOC_MAX (1 << 20)
+int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8_t* mat2, const double* gam,
+                              const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n);
+
 /* ---- measurement ----
  * pgdg_profile: record CUDA events on the context stream around every method
  * call; pgdg_profile_read returns per-method totals (names ';'-separated, in

@@ -22,6 +22,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/pgdg.h"
@@ -530,6 +531,40 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
   if (n < 0 || !in6 || !mat2 || !gam || !pinf || !out3 || nmat < 1) return PGDG_EINVAL;
   if (n == 0) return PGDG_OK;
   return mgfm_seeded_run((void*)net, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr, 0);
+}
+
+/* Seeds of pgdg_mgfm_batched_noalloc: a file-scope device array, so the call
+ * itself never allocates (see the declaration for which callers need that).
+ * Its address is looked up once per device. */
+static __device__ __align__(256) double g_noalloc_seeds[PGDG_MGFM_NOALLOC_MAX];
+
+int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8_t* mat2, const double* gam,
+                              const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n) {
+  if (n < 0 || !in6 || !mat2 || !gam || !pinf || !out3 || nmat < 1) return PGDG_EINVAL;
+  if (n > PGDG_MGFM_NOALLOC_MAX) return PGDG_EOVERFLOW;
+  if (n == 0) return PGDG_OK;
+  const double* sd = nullptr;
+  if (net) {
+    constexpr int MAXDEV = 64;
+    static double* seeds_of[MAXDEV] = {};
+    static std::mutex mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV) return PGDG_ECUDA;
+    double* seeds = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      if (!seeds_of[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_seeds) != cudaSuccess || !p) return PGDG_ECUDA;
+        seeds_of[dev] = static_cast<double*>(p);
+      }
+      seeds = seeds_of[dev];
+    }
+    seed_launch(const_cast<pgdg_mlp*>(net), in6, mat2, gam, pinf, variant, seeds, n, 0);
+    sd = seeds;
+  }
+  k_mgfm_seeded<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, nullptr);
+  return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 
 }  // extern "C"

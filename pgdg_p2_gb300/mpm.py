@@ -63,6 +63,7 @@ def lib():
         L.pgdg_launch_count.argtypes = [vp, P(C.c_int64)]
         L.pgdg_time_advance.argtypes = [vp, C.c_int, P(C.c_double)]
         L.pgdg_mgfm_batched.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int64]
+        L.pgdg_mgfm_batched_noalloc.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int64]
         L.pgdg_surrogate_create.argtypes = [C.c_int, P(vp)]
         L.pgdg_surrogate_destroy.argtypes = [vp]
         L.pgdg_surrogate_num_params.restype = C.c_int

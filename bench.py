@@ -200,6 +200,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms / args.steps,
                               "gpu_launches": launches, "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
+                              "tuning": {"pst_variant": g.tune("pst")},
                               "note": "timed region only"}), flush=True)
         g.close()
         return
@@ -311,6 +312,7 @@ def run_ours(args):
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
                 "cpu_baseline": cpu, "fp64_path": fp64, "ablation": ablation, "mgfm_c5": c5,
                 "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
+                "tuning": {"pst_variant": g.tune("pst")},
                 "stats": {k: st[k] for k in ("n_particles", "n_split", "n_merge", "n_inlet", "n_outlet",
                                              "mgfm_calls", "mgfm_iters", "g2p_fallbacks", "list_entries")}}
         print(json.dumps(line), flush=True)

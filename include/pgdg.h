@@ -146,6 +146,14 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
 int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8_t* mat2, const double* gam,
                               const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n);
 
+/* ---- kernel variants (no reference counterpart) ----
+ * Some kernels have several implementations with identical results; the
+ * context times them on its own state at their first call and keeps the
+ * fastest.  kernel: "pst" (the shifting kernel of pgdg_update_particle).
+ * variant >= 0 forces that variant, -1 re-tunes at the next call, -2 only
+ * queries; *chosen (may be NULL) receives the current choice (-1: not tuned). */
+int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen);
+
 /* ---- measurement ----
  * pgdg_profile: record CUDA events on the context stream around every method
  * call; pgdg_profile_read returns per-method totals (names ';'-separated, in

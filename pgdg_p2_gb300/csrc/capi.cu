@@ -28,6 +28,7 @@ struct pgdg_ctx {
   int precision = PGDG_PREC_FP64;
   void* net = nullptr;   /* attached seed surrogate (pgdg_mlp) */
   int iface_queue = 0;   /* 1: interface problems solved as one batch */
+  int pst_var = -1;      /* shifting-kernel variant (-1: tune at the next call) */
   int64_t iface_last = 0;
   virtual int iface_download(double*, int8_t*, int64_t, int64_t*) = 0;
   int64_t iterate = 0;
@@ -806,6 +807,31 @@ struct Ctx : pgdg_ctx {
     }
     return PGDG_OK;
   }
+  /* autotuner: time each variant of a kernel twice on the current state (the
+   * kernel must only overwrite its outputs, and all variants give the same
+   * results) and keep the fastest */
+  template <class F>
+  int tune(int nvar, F&& run) {
+    if (nvar <= 1) return 0;
+    cudaEvent_t a = ev_get(), b = ev_get();
+    float best = 0.f;
+    int bv = 0;
+    for (int v = 0; v < nvar; v++) {
+      run(v);
+      cudaEventRecord(a, st);
+      run(v);
+      run(v);
+      cudaEventRecord(b, st);
+      if (cudaEventSynchronize(b) != cudaSuccess) return 0;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (v == 0 || ms < best) {
+        best = ms;
+        bv = v;
+      }
+    }
+    return bv;
+  }
   int grow_queue(int64_t need) {
     for (void* p : {(void*)Q.in6, (void*)Q.mat, (void*)Q.out3}) {
       for (auto& a : allocs)
@@ -858,7 +884,9 @@ struct Ctx : pgdg_ctx {
       if (xn == xs || xn == x0 || xn < 0 || xn > 2) xn = (xs + 1) % 3;  /* md 1 without md 0 */
     }
     timed("g2p", 1, [&] { Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, st); });
-    timed("pst", 1, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, st); });
+    if (pst_var < 0)
+      pst_var = tune(Launch<D, R, EX>::pst_variants(), [&](int v) { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, v, st); });
+    timed("pst", 1, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, pst_var, st); });
     if (md == 1) timed("store_lists", 2, [&] { Launch<D, R, EX>::store_lists(K, P, xs, hs, xn, st); });
     P.xb = xn;
     P.hb = hn;
@@ -965,6 +993,16 @@ int pgdg_set_surrogate(pgdg_ctx* ctx, pgdg_mlp* net) {
   }
   ctx->net = (void*)net;
   ctx->iface_queue = net ? 1 : ctx->iface_queue;
+  return PGDG_OK;
+}
+int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen) {
+  if (!kernel || std::strcmp(kernel, "pst") != 0 || variant < -2) {
+    ctx->err = "tunable kernels: pst; variant >= -2";
+    return PGDG_EINVAL;
+  }
+  if (variant >= 0) ctx->pst_var = variant;
+  else if (variant == -1) ctx->pst_var = -1;
+  if (chosen) *chosen = ctx->pst_var;
   return PGDG_OK;
 }
 int pgdg_set_iface_queue(pgdg_ctx* ctx, int on) {

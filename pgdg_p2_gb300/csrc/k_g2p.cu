@@ -176,13 +176,13 @@ struct PstSmem {
 };
 
 template <int D, typename R>
-__host__ __device__ inline size_t pst_smem_bytes(int nsc, int nrow, int cap) {
+__host__ __device__ inline size_t pst_smem_bytes(int nsc, int nrow, int cap, bool queue = true) {
   size_t b = sizeof(int) * (size_t)(3 * nsc + 1);
   b = (b + 31) / 32 * 32;
   b += sizeof(R) * (size_t)(2 * D * nsc);
   b = (b + 31) / 32 * 32;
   b += 4 * sizeof(R) * (size_t)cap;
-  b += sizeof(unsigned short) * (size_t)PST_BUF * PST_THREADS;
+  if (queue) b += sizeof(unsigned short) * (size_t)PST_BUF * PST_THREADS;
   b += sizeof(R) * (size_t)(4 * nrow);
   b += (size_t)cap;
   return b + 128;
@@ -298,6 +298,18 @@ __device__ __forceinline__ void pst_fluid(const DevPtrs<R>& P, int32_t q, const 
   if (pp.member(xsq)) pst_rec<D, R, EX>(P, q, pp);
 }
 
+/* warp-wide min / max of a coordinate over the lanes of mask (as float, rounded
+ * outward, through order-preserving integer keys) */
+__device__ __forceinline__ int fkey(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float fkey_inv(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7FFFFFFF); }
+__device__ __forceinline__ float warp_min_lo(unsigned mask, float x) { return fkey_inv(__reduce_min_sync(mask, fkey(x))); }
+__device__ __forceinline__ float warp_max_hi(unsigned mask, float x) { return fkey_inv(__reduce_max_sync(mask, fkey(x))); }
+__device__ __forceinline__ float warp_min_lo(unsigned mask, double x) { return warp_min_lo(mask, __double2float_rd(x)); }
+__device__ __forceinline__ float warp_max_hi(unsigned mask, double x) { return warp_max_hi(mask, __double2float_ru(x)); }
+
 template <typename R>
 __device__ __forceinline__ int slot_of(R w);
 template <>
@@ -306,7 +318,7 @@ template <>
 __device__ __forceinline__ int slot_of<double>(double w) { return (int)w; }
 
 /* one particle: neighbour sum, Bound_pen, Update_PST; sm == nullptr -> global path */
-template <int D, typename R, bool EX>
+template <int D, typename R, bool EX, int VAR>
 __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, const R* XS, const R* XN, const R* HS,
                              const R* HN, R dt, R max_v, const PstSmem<D, R>* sm) {
   PstPart<D, R, EX> pp;
@@ -337,7 +349,20 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
     int nbuf = 0;
     /* sum the queued members in queue (= scan) order */
     auto flush = [&]() {
-      for (int i = 0; i < nbuf; i++) {
+      using V4 = typename Vec4<R>::T;
+      int i = 0;
+      for (; i + 1 < nbuf; i += 2) {
+        /* two records in flight before either is summed (order kept) */
+        const int e0 = sm->buf[i * PST_THREADS + threadIdx.x];
+        const int e1 = sm->buf[(i + 1) * PST_THREADS + threadIdx.x];
+        const V4* r0 = reinterpret_cast<const V4*>(P.rec + 8 * (int64_t)slot_of<R>(sm->ent[e0].w));
+        const V4* r1 = reinterpret_cast<const V4*>(P.rec + 8 * (int64_t)slot_of<R>(sm->ent[e1].w));
+        const V4 a0 = r0[0], b0 = r0[1], a1 = r1[0], b1 = r1[1];
+        R x0[3] = {a0.x, a0.y, a0.z}, x1[3] = {a1.x, a1.y, a1.z};
+        pp.add(x0, a0.w, b0.x, b0.y, (int)b0.z, nullptr);
+        pp.add(x1, a1.w, b1.x, b1.y, (int)b1.z, nullptr);
+      }
+      if (i < nbuf) {
         const int e = sm->buf[i * PST_THREADS + threadIdx.x];
         pst_rec<D, R, EX>(P, slot_of<R>(sm->ent[e].w), pp);
       }
@@ -352,18 +377,21 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
       }
     };
     if constexpr (!EX) {
-      /* mixed / FMA paths: for each row of cells along the last axis whose
-       * bounds in the other axes come within 2h, only the entries whose row
-       * coordinate lies within the sphere's chord are tested (binary search in
-       * the sorted row); the cell tag keeps the scan to the particle's
-       * +-rad2 cell window.  Boundary particles follow in a second pass (the
-       * summation order only affects rounding). */
+      if constexpr (VAR != 1) {
+      /* variants 0, 2 and 3, per lane: for each row of cells along the last axis (z in
+       * 3D, y in 2D) whose bounds in the other axes come within 2h, only the
+       * entries whose row coordinate lies within the chord of the 2h sphere are
+       * tested (binary search in the sorted row); the cell tag keeps the scan
+       * to the particle's +-rad2 cell window.  Variant 0 queues the members and
+       * sums them in warp-wide batches; variants 2 and 3 sum each member as it
+       * is found (no queue, less shared memory; 3 is launched for 3 blocks per
+       * SM). */
       constexpr int RA = D - 1;
       const int clo = lo[RA] - sm->lo[RA], chi = hi[RA] - sm->lo[RA];
       const R zp = pp.xsp[RA];
-      const int t1 = (D == 3) ? hi[1] : lo[1];
+      const int u1 = (D == 3) ? hi[1] : lo[1];
       for (int t = lo[0]; t <= hi[0]; t++)
-        for (int u = lo[1]; u <= t1; u++) {
+        for (int u = lo[1]; u <= u1; u++) {
           const int row = (D == 3) ? (t - sm->lo[0]) * sm->n[1] + (u - sm->lo[1]) : (t - sm->lo[0]);
           R dxy = R(0);
           for (int d = 0; d < D - 1; d++) {
@@ -375,9 +403,9 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
             const R w = sqrt_r<R>(lim2m - dxy); /* half chord of the 2h sphere */
             const R za = zp - w, zb = zp + w;
             const int rl = row * sm->n[RA];
-            int e = sm->off[rl], e1 = sm->off[rl + sm->n[RA]];
-            int hi_e = e1;
-            while (e < hi_e) {   /* first entry with coordinate >= za */
+            int e = sm->off[rl], hi_e = sm->off[rl + sm->n[RA]];
+            const int e1 = hi_e;
+            while (e < hi_e) { /* first entry with coordinate >= za */
               const int m = (e + hi_e) >> 1;
               const R zm = (RA == 2) ? sm->ent[m].z : sm->ent[m].y;
               if (zm < za) e = m + 1;
@@ -391,13 +419,81 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
               if (ce < clo || ce > chi) continue;
               R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
               if (pp.member(xsq)) {
+                if constexpr (VAR >= 2) {
+                  pst_rec<D, R, EX>(P, slot_of<R>(v.w), pp); /* summed at once, same order */
+                } else {
+                  if (nbuf == PST_BUF) flush();
+                  sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
+                }
+              }
+            }
+          }
+          if constexpr (VAR < 2)
+            if (__any_sync(__activemask(), nbuf >= PST_BUF / 2)) flush();
+        }
+      } else {
+      /* variant 1, warp-cooperative: the lanes walk the union of their
+       * rows of cells along the last axis (z in 3D, y in 2D) together, and in
+       * each row the union of their windows of the sorted row coordinate (the
+       * chord of each lane's 2h sphere); every staged entry is one broadcast
+       * shared-memory read that each lane tests against its own sphere and
+       * +-rad2 cell window.  A lane's members are queued in the same order as
+       * a per-lane scan would queue them.  Boundary particles follow in a
+       * second pass (the summation order only affects rounding). */
+      constexpr int RA = D - 1;
+      const unsigned am = __activemask();
+      const int clo = lo[RA] - sm->lo[RA], chi = hi[RA] - sm->lo[RA];
+      const R zp = pp.xsp[RA];
+      const int t0 = __reduce_min_sync(am, lo[0]), t1 = __reduce_max_sync(am, hi[0]);
+      const int u0 = (D == 3) ? __reduce_min_sync(am, lo[1]) : 0;
+      const int u1 = (D == 3) ? __reduce_max_sync(am, hi[1]) : 0;
+      for (int t = t0; t <= t1; t++)
+        for (int u = u0; u <= u1; u++) {
+          const int row = (D == 3) ? (t - sm->lo[0]) * sm->n[1] + (u - sm->lo[1]) : (t - sm->lo[0]);
+          bool need = t >= lo[0] && t <= hi[0] && (D == 2 || (u >= lo[1] && u <= hi[1]));
+          R za = R(1e30), zb = R(-1e30);
+          if (need) {
+            R dxy = R(0);
+            for (int d = 0; d < D - 1; d++) {
+              R a = sm->rlo[2 * row + d] - pp.xsp[d], b = pp.xsp[d] - sm->rhi[2 * row + d];
+              R w = a > b ? a : b;
+              if (w > R(0)) dxy += w * w;
+            }
+            if (dxy <= lim2m) {
+              const R w = sqrt_r<R>(lim2m - dxy); /* half chord of the 2h sphere */
+              za = zp - w;
+              zb = zp + w;
+            } else {
+              need = false;
+            }
+          }
+          if (!__any_sync(am, need)) continue;
+          const float fa = warp_min_lo(am, za), fb = warp_max_hi(am, zb);
+          const int rl = row * sm->n[RA];
+          int e = sm->off[rl], hi_e = sm->off[rl + sm->n[RA]];
+          const int e1 = hi_e;
+          while (e < hi_e) { /* first entry with coordinate >= the union's lower end */
+            const int m = (e + hi_e) >> 1;
+            const R zm = (RA == 2) ? sm->ent[m].z : sm->ent[m].y;
+            if (zm < R(fa)) e = m + 1;
+            else hi_e = m;
+          }
+          for (; e < e1; e++) {
+            const auto v = sm->ent[e];
+            const R zv = (RA == 2) ? v.z : v.y;
+            if (zv > R(fb)) break;
+            const int ce = sm->ecell[e];
+            if (need && ce >= clo && ce <= chi) {
+              R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
+              if (pp.member(xsq)) {
                 if (nbuf == PST_BUF) flush();
                 sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
               }
             }
           }
-          if (__any_sync(__activemask(), nbuf >= PST_BUF / 2)) flush();
+          if (__any_sync(am, nbuf >= PST_BUF / 2)) flush();
         }
+      }
       flush();
       bool edge = false;
       for (int d = 0; d < D; d++) edge = edge || lo[d] == 0 || hi[d] == K.N[d] - 1;
@@ -511,8 +607,8 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
   }
 }
 
-template <int D, typename R, bool EX>
-__global__ void __launch_bounds__(PST_THREADS, 2) k_pst(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn,
+template <int D, typename R, bool EX, int VAR>
+__global__ void __launch_bounds__(PST_THREADS, (VAR == 3 ? 3 : 2)) k_pst(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn,
                                                     int nb0, int nb1, int cap) {
   using BK = Brick<D>;
   using V4 = typename Vec4<R>::T;
@@ -553,7 +649,7 @@ __global__ void __launch_bounds__(PST_THREADS, 2) k_pst(CaseK K, DevPtrs<R> P, i
   sm.ent = reinterpret_cast<V4*>(smem_raw + o);
   sm.buf = reinterpret_cast<unsigned short*>(sm.ent + cap);
   sm.nrow = (D == 3) ? sm.n[0] * sm.n[1] : sm.n[0];
-  sm.rlo = reinterpret_cast<R*>(sm.buf + (size_t)PST_BUF * PST_THREADS);
+  sm.rlo = reinterpret_cast<R*>(sm.buf + (VAR >= 2 && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
   sm.rhi = sm.rlo + 2 * sm.nrow;
   sm.ecell = reinterpret_cast<unsigned char*>(sm.rhi + 2 * sm.nrow);
   __shared__ int s_total, s_maxcnt;
@@ -691,12 +787,12 @@ __global__ void __launch_bounds__(PST_THREADS, 2) k_pst(CaseK K, DevPtrs<R> P, i
     while (s_boff[q + 1] <= i) q++;
     const int64_t c = s_bcell[q];
     const int32_t p = P.bucket[c * K.maxpc + (i - s_boff[q])];
-    pst_particle<D, R, EX>(K, P, p, XS, XN, HS, HN, dt, max_v, use_sm ? &sm : nullptr);
+    pst_particle<D, R, EX, VAR>(K, P, p, XS, XN, HS, HN, dt, max_v, use_sm ? &sm : nullptr);
   }
 }
 
-template <int D, typename R, bool EX>
-void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, cudaStream_t st) {
+template <int D, typename R, bool EX, int VAR>
+static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, cudaStream_t st) {
   using BK = Brick<D>;
   const int nb0 = (D == 3) ? (K.N[2] + BK::B2 - 1) / BK::B2 : 1;
   const int nb1 = (K.N[1] + BK::B1 - 1) / BK::B1;
@@ -705,24 +801,50 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
   const int nsc = (BK::B0 + 2 * r) * (BK::B1 + 2 * r) * (D == 3 ? BK::B2 + 2 * r : 1);
   const int ppc = (D == 3) ? 8 : 4;
   const int nrow = (D == 3) ? (BK::B0 + 2 * r) * (BK::B1 + 2 * r) : (BK::B0 + 2 * r);
-  int cap = nsc * ppc * 5 / 4;
+  const bool queue = EX || VAR < 2;
+  /* staging headroom over the nominal count (split children); variant 3 keeps
+   * it at 1/8 so three blocks fit in an SM's shared memory */
+  int cap = (!EX && VAR == 3) ? nsc * ppc * 9 / 8 : nsc * ppc * 5 / 4;
   if (cap > 65535) cap = 65535;
-  size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap);
+  size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, queue);
   while (bytes > 220 * 1024 && cap > 256) {
     cap = cap * 3 / 4;
-    bytes = pst_smem_bytes<D, R>(nsc, nrow, cap);
+    bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, queue);
   }
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_pst<D, R, EX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 224 * 1024);
+    cudaFuncSetAttribute(k_pst<D, R, EX, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 224 * 1024);
     attr_set = true;
   }
-  k_pst<D, R, EX><<<nbx * nb1 * nb0, PST_THREADS, bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap);
+  k_pst<D, R, EX, VAR><<<nbx * nb1 * nb0, PST_THREADS, bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap);
+}
+
+/* variants of the shifting kernel (identical results; the context's autotuner
+ * times them on its own state and keeps the fastest): 0 per-lane row scan with
+ * queued members, 1 warp-cooperative row scan, 2 per-lane scan summing members
+ * at once, 3 the same for 3 blocks per SM.  The exact path has one. */
+template <int D, typename R, bool EX>
+int Launch<D, R, EX>::pst_variants() {
+  return EX ? 1 : 4;
+}
+
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, int var,
+                           cudaStream_t st) {
+  if constexpr (EX) {
+    pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, st);
+  } else {
+    if (var == 1) pst_launch<D, R, EX, 1>(K, P, xs, hs, xn, hn, st);
+    else if (var == 2) pst_launch<D, R, EX, 2>(K, P, xs, hs, xn, hn, st);
+    else if (var == 3) pst_launch<D, R, EX, 3>(K, P, xs, hs, xn, hn, st);
+    else pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, st);
+  }
 }
 
 #define PGDG_INST(D, R, EX)                                                                              \
   template void Launch<D, R, EX>::g2p(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, cudaStream_t); \
-  template void Launch<D, R, EX>::pst(const CaseK&, const DevPtrs<R>&, int, int, int, int, cudaStream_t);
+  template void Launch<D, R, EX>::pst(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, cudaStream_t); \
+  template int Launch<D, R, EX>::pst_variants();
 #ifdef PGDG_EXACT_TU
 PGDG_INST(2, double, true)
 PGDG_INST(3, double, true)

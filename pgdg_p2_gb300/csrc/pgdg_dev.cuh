@@ -209,7 +209,8 @@ struct Launch {
   /* xs/hs: stage-start coordinate/h buffers, x0: step-start coordinates (md 1),
    * xn/hn: buffers receiving the new coordinates/h */
   static void g2p(const CaseK&, const DevPtrs<R>&, int md, int xs, int x0, int xn, int hn, cudaStream_t);
-  static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, cudaStream_t);
+  static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, int var, cudaStream_t);
+  static int pst_variants();
 };
 
 /* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls, iterations, cap hits) */

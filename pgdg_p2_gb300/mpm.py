@@ -75,6 +75,7 @@ def lib():
         L.pgdg_surrogate_train_step.argtypes = [vp, vp, vp, C.c_int64, C.c_float, P(C.c_double)]
         L.pgdg_set_surrogate.argtypes = [vp, vp]
         L.pgdg_set_iface_queue.argtypes = [vp, C.c_int]
+        L.pgdg_tune.argtypes = [vp, C.c_char_p, C.c_int, P(C.c_int)]
         L.pgdg_iface_download.argtypes = [vp, vp, vp, C.c_int64, P(C.c_int64)]
         _lib = L
     return _lib
@@ -209,6 +210,13 @@ class MPM:
     def set_surrogate(self, net):
         """Seed every interface MGFM solve of the mixed step with `net` (None: plain)."""
         self._ck(lib().pgdg_set_surrogate(self.h, net.h if net is not None else None), "set_surrogate")
+
+    def tune(self, kernel="pst", variant=-2):
+        """Force (variant >= 0), re-tune (-1) or query (-2) a kernel's variant;
+        returns the current choice (-1: not tuned yet)."""
+        ch = C.c_int()
+        self._ck(lib().pgdg_tune(self.h, kernel.encode(), int(variant), C.byref(ch)), "tune")
+        return ch.value
 
     def set_iface_queue(self, on):
         """Solve each stage's interface problems as one batch (mixed / FP64_FMA paths)."""

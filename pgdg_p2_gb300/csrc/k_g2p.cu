@@ -40,6 +40,17 @@ __global__ void __launch_bounds__(128) k_g2p(CaseK K, DevPtrs<R> P, int md, int 
   R* XN = P.X[xn];
   R* HN = P.H[hn];
   unsigned long long nfb = 0;
+  /* case constants in R, converted once per thread */
+  R blr[3], psr[3], gam_r[F], pf_r[F], pfe_r[F];
+  for (int d = 0; d < 3; d++) {
+    blr[d] = R(K.bl[d]);
+    psr[d] = R(K.ps[d]);
+  }
+  for (int s = 0; s < F; s++) {
+    gam_r[s] = (R)K.gamma[s];
+    pf_r[s] = (R)K.pinf[s];
+    pfe_r[s] = (R)K.pinf_eos[s];
+  }
   GRID_STRIDE(p, n) {
     const int ph = P.phase[p];
     if (ph == 0) continue;
@@ -63,7 +74,7 @@ __global__ void __launch_bounds__(128) k_g2p(CaseK K, DevPtrs<R> P, int md, int 
     idx[1] = (int)((ci / K.N[2]) % K.N[1]);
     idx[0] = (int)(ci / ((int64_t)K.N[1] * K.N[2]));
     R dri[3];
-    for (int d = 0; d < D; d++) dri[d] = x[d] - (R(K.bl[d]) + R(K.ps[d]) * R(idx[d] + 0.5));
+    for (int d = 0; d < D; d++) dri[d] = x[d] - (blr[d] + psr[d] * ((R)idx[d] + R(0.5)));
     R Ui[U];
     for (int t = 0; t < U; t++) {
       R acc = P.ccoef[((ss * U + t) * B + 1) * nc + ci] * dri[0];
@@ -77,8 +88,8 @@ __global__ void __launch_bounds__(128) k_g2p(CaseK K, DevPtrs<R> P, int md, int 
       v[k] = rhov[k] / rho;
       sq = (k == 0) ? v[k] * v[k] : sq + v[k] * v[k];
     }
-    const R g = (R)K.gamma[ss], pf = (R)K.pinf[ss];
-    R Pp = eos_p<R>(E - R(0.5) * rho * sq, g, (R)K.pinf_eos[ss]);
+    const R g = gam_r[ss], pf = pf_r[ss];
+    R Pp = eos_p<R>(E - R(0.5) * rho * sq, g, pfe_r[ss]);
     R c = sqrt_r<R>(g * (pf + Pp) / rho);
     bool fb = (Pp < R(-0.05) * pf || rho < R(0));
     for (int t = 0; t < U; t++)

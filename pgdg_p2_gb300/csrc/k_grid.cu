@@ -64,6 +64,52 @@ __device__ __forceinline__ void face(const CaseK& K, const int* idx, const doubl
   fc.bound = inside ? 0 : K.bc[side];
 }
 
+/* The same face in the stage type R relative to the cell centre, for the
+ * non-exact paths: centre offset, tangent half-vectors and area come from the
+ * half cell sizes hps (no absolute coordinates, no FP64 arithmetic); Sax[a] is
+ * the area of a face normal to axis a. */
+template <typename R>
+struct FaceRel {
+  int axis, bound, nb[3];
+  R sgn, cen[3], t0[3], t1[3], S;
+};
+template <int D, typename R>
+__device__ __forceinline__ void face_rel(const CaseK& K, const int* idx, const R* hps, const R* Sax, int f,
+                                         FaceRel<R>& fc) {
+  for (int d = 0; d < 3; d++) {
+    fc.cen[d] = fc.t0[d] = fc.t1[d] = R(0);
+    fc.nb[d] = idx[d];
+  }
+  int side;
+  switch (f) {
+    case 0: fc.axis = 1; fc.sgn = R(-1); fc.t0[0] = hps[0]; fc.t1[2] = hps[2]; fc.cen[1] = -hps[1]; fc.nb[1] -= 1; side = 2; break;
+    case 1: fc.axis = 0; fc.sgn = R(1); fc.t0[1] = hps[1]; fc.t1[2] = hps[2]; fc.cen[0] = hps[0]; fc.nb[0] += 1; side = 1; break;
+    case 2: fc.axis = 1; fc.sgn = R(1); fc.t0[0] = -hps[0]; fc.t1[2] = hps[2]; fc.cen[1] = hps[1]; fc.nb[1] += 1; side = 3; break;
+    case 3: fc.axis = 0; fc.sgn = R(-1); fc.t0[1] = -hps[1]; fc.t1[2] = hps[2]; fc.cen[0] = -hps[0]; fc.nb[0] -= 1; side = 0; break;
+    case 4: fc.axis = 2; fc.sgn = R(-1); fc.t0[0] = hps[0]; fc.t1[1] = hps[1]; fc.cen[2] = -hps[2]; fc.nb[2] -= 1; side = 4; break;
+    default: fc.axis = 2; fc.sgn = R(1); fc.t0[0] = hps[0]; fc.t1[1] = hps[1]; fc.cen[2] = hps[2]; fc.nb[2] += 1; side = 5; break;
+  }
+  if (D == 2) fc.t1[2] = R(0);
+  fc.S = Sax[fc.axis];
+  bool inside = true;
+  for (int d = 0; d < D; d++) inside = inside && fc.nb[d] >= 0 && fc.nb[d] < K.N[d];
+  fc.bound = inside ? 0 : K.bc[side];
+}
+/* half cell sizes and face areas in R */
+template <int D, typename R>
+__device__ __forceinline__ void cell_geom(const CaseK& K, R* hps, R* Sax) {
+  for (int d = 0; d < 3; d++) hps[d] = (R)(0.5 * K.ps[d]);
+  if (D == 3) {
+    Sax[0] = (R)(K.ps[1] * K.ps[2]);
+    Sax[1] = (R)(K.ps[0] * K.ps[2]);
+    Sax[2] = (R)(K.ps[1] * K.ps[0]);
+  } else {
+    Sax[0] = (R)K.ps[1];
+    Sax[1] = (R)K.ps[0];
+    Sax[2] = R(0);
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* Used_state_update (mpm.cpp:184-263)                                */
 /* ------------------------------------------------------------------ */
@@ -358,12 +404,18 @@ template <int D, typename R, bool EX>
 __global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
   constexpr int U = D + 2, B = D + 1, NF = 2 * D;
   const int64_t nc = K.ncell;
+  R hps[3], Sax[3];
+  cell_geom<D, R>(K, hps, Sax);
+  /* positivity probe offsets, converted once per block */
+  __shared__ R s_probe[8][3];
+  if (threadIdx.x < 24) s_probe[threadIdx.x / 3][threadIdx.x % 3] = (R)K.probe[threadIdx.x / 3][threadIdx.x % 3];
+  __syncthreads();
   GRID_STRIDE(ci, nc) {
     if (!P.cused[ci]) continue;
     int idx[3];
     cijk<D>(K, ci, idx);
     double xc[3];
-    center<D>(K, idx, xc);
+    if constexpr (EX) center<D>(K, idx, xc);
     R u_max[F][U], u_min[F][U], pi[F][U], lim[F][U];
     for (int s = 0; s < F; s++)
       for (int u = 0; u < U; u++) {
@@ -399,8 +451,19 @@ __global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
     const bool mirror_j = (idx[1] == K.N[1] - 1 || idx[1] == 0);
     const bool mirror_k = (D == 3) && (idx[2] == K.N[2] - 1 || idx[2] == 0);
     for (int f = 0; f < NF; f++) {
-      FaceK fc;
-      face<D>(K, idx, xc, f, fc);
+      int fcb, fnb[3];
+      if constexpr (EX) {
+        FaceK fc;
+        face<D>(K, idx, xc, f, fc);
+        fcb = fc.bound;
+        for (int d = 0; d < 3; d++) fnb[d] = fc.nb[d];
+      } else {
+        FaceRel<R> fc;
+        face_rel<D, R>(K, idx, hps, Sax, f, fc);
+        fcb = fc.bound;
+        for (int d = 0; d < 3; d++) fnb[d] = fc.nb[d];
+      }
+      struct { int bound; int nb[3]; } fc = {fcb, {fnb[0], fnb[1], fnb[2]}};
       if (fc.bound == 0) {
         int64_t nb = cidx3(K, fc.nb[0], fc.nb[1], fc.nb[2]);
         for (int s = 0; s < F; s++) {
@@ -461,16 +524,27 @@ __global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
         u_min[s][u] = amin1(u_min[s][u], R(0.));
       }
     for (int f = 0; f < NF; f++) {
-      FaceK fc;
-      face<D>(K, idx, xc, f, fc);
       R dr[3];
-      if (fc.bound == 0) {
-        double xn[3];
-        center<D>(K, fc.nb, xn);
-        for (int d = 0; d < D; d++) dr[d] = (R)(xn[d] - xc[d]);
+      int fbound;
+      if constexpr (EX) {
+        FaceK fc;
+        face<D>(K, idx, xc, f, fc);
+        fbound = fc.bound;
+        if (fc.bound == 0) {
+          double xn[3];
+          center<D>(K, fc.nb, xn);
+          for (int d = 0; d < D; d++) dr[d] = (R)(xn[d] - xc[d]);
+        } else {
+          for (int d = 0; d < D; d++) dr[d] = (R)(fc.cen[d] - xc[d]);
+        }
       } else {
-        for (int d = 0; d < D; d++) dr[d] = (R)(fc.cen[d] - xc[d]);
+        FaceRel<R> fc;
+        face_rel<D, R>(K, idx, hps, Sax, f, fc);
+        fbound = fc.bound;
+        /* neighbour centre (interior) or face centre (boundary) from the cell centre */
+        for (int d = 0; d < D; d++) dr[d] = (fc.bound == 0) ? R(2) * fc.cen[d] : fc.cen[d];
       }
+      (void)fbound;
       for (int s = 0; s < F; s++) {
         int lim_fg = bd_fg;
         if (P.calph[s * nc + ci] != R(1)) lim_fg = 1;
@@ -498,7 +572,7 @@ __global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
           R acc = R(0);
           for (int b = 0; b < D; b++) {
             R cf = P.ccoef[((s * U + u) * B + 1 + b) * nc + ci];
-            acc = (b == 0) ? cf * (R)K.probe[pr][b] : acc + cf * (R)K.probe[pr][b];
+            acc = (b == 0) ? cf * s_probe[pr][b] : acc + cf * s_probe[pr][b];
           }
           Ui[u] = P.ccoef[((s * U + u) * B) * nc + ci] + lim[s][u] * acc;
         }
@@ -546,13 +620,19 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
   constexpr int U = D + 2, B = D + 1, NF = 2 * D, NQ = (D == 3) ? 4 : 2, NG = (D == 3) ? 8 : 4;
   const int64_t nc = K.ncell;
   const double gp[2] = {-1. / sqrt(3.), 1. / sqrt(3.)};
+  /* the non-exact paths take the cell geometry in R, relative to the centre */
+  const R gpr[2] = {R(-1. / sqrt(3.)), R(1. / sqrt(3.))};
+  R hps[3], Sax[3];
+  cell_geom<D, R>(K, hps, Sax);
+  const R inv[4] = {R(1. / (voli_d + 1e-20)), R(1. / (mij1 + 1e-20)), R(1. / (mij2 + 1e-20)),
+                    R(1. / (mij3 + 1e-20))};
   unsigned long long ncall = 0, nit = 0, nmax = 0;
   GRID_STRIDE(ci, nc) {
     if (!P.cused[ci]) continue;
     int idx[3];
     cijk<D>(K, ci, idx);
     double xc[3];
-    center<D>(K, idx, xc);
+    if constexpr (EX) center<D>(K, idx, xc);
     const bool mirror_j = (idx[1] == K.N[1] - 1 || idx[1] == 0);
     const bool mirror_k = (D == 3) && (idx[2] == K.N[2] - 1 || idx[2] == 0);
     int64_t qi = 0;
@@ -577,7 +657,16 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
       const R voli = (R)voli_d;
       for (int g = 0; g < (MODE == 2 ? 0 : NG); g++) {
         int g1 = (D == 3) ? (g >> 2) : (g >> 1), g2 = (D == 3) ? ((g >> 1) & 1) : (g & 1), g3 = g & 1;
-        R dp[3] = {(R)(gp[g1] * (K.ps[0] / 2)), (R)(gp[g2] * (K.ps[1] / 2)), (D == 3) ? (R)(gp[g3] * (K.ps[2] / 2)) : R(0)};
+        R dp[3];
+        if constexpr (EX) {
+          dp[0] = (R)(gp[g1] * (K.ps[0] / 2));
+          dp[1] = (R)(gp[g2] * (K.ps[1] / 2));
+          dp[2] = (D == 3) ? (R)(gp[g3] * (K.ps[2] / 2)) : R(0);
+        } else {
+          dp[0] = gpr[g1] * hps[0];
+          dp[1] = gpr[g2] * hps[1];
+          dp[2] = (D == 3) ? gpr[g3] * hps[2] : R(0);
+        }
         const R gw = (D == 3) ? R(0.125) : R(0.25);
         R Up[U];
         for (int u = 0; u < U; u++) {
@@ -598,24 +687,36 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
       }
       /* face integral */
       for (int f = 0; f < NF; f++) {
+        /* exact path: the reference's absolute FP64 face geometry; otherwise
+         * the same face relative to the cell centre in R */
         FaceK fc;
-        face<D>(K, idx, xc, f, fc);
-        const int a = fc.axis;
-        const R na = (R)fc.sgn;
+        FaceRel<R> fr;
+        if constexpr (EX) face<D>(K, idx, xc, f, fc);
+        else face_rel<D, R>(K, idx, hps, Sax, f, fr);
+        const int a = EX ? fc.axis : fr.axis;
+        const int fbound = EX ? fc.bound : fr.bound;
+        const int* fnb = EX ? fc.nb : fr.nb;
+        const R na = EX ? (R)fc.sgn : fr.sgn;
         R DFn[B][U];
         for (int b = 0; b < B; b++)
           for (int u = 0; u < U; u++) DFn[b][u] = R(0);
         int64_t nb = -1;
-        if (fc.bound == 0) nb = cidx3(K, fc.nb[0], fc.nb[1], fc.nb[2]);
+        if (fbound == 0) nb = cidx3(K, fnb[0], fnb[1], fnb[2]);
         double xn[3] = {0, 0, 0};
-        if (nb >= 0) center<D>(K, fc.nb, xn);
+        if constexpr (EX)
+          if (nb >= 0) center<D>(K, fc.nb, xn);
         for (int qd = 0; qd < NQ; qd++) {
           int g1 = (D == 3) ? (qd >> 1) : qd, g2 = qd & 1;
           double dpv[3];
-          for (int d = 0; d < 3; d++) dpv[d] = (D == 3) ? gp[g1] * fc.t0[d] + gp[g2] * fc.t1[d] : gp[g1] * fc.t0[d];
           const R gw = (D == 3) ? R(0.25) : R(0.5);
           R dri[3];
-          for (int d = 0; d < D; d++) dri[d] = (R)(dpv[d] + fc.cen[d] - xc[d]);
+          if constexpr (EX) {
+            for (int d = 0; d < 3; d++) dpv[d] = (D == 3) ? gp[g1] * fc.t0[d] + gp[g2] * fc.t1[d] : gp[g1] * fc.t0[d];
+            for (int d = 0; d < D; d++) dri[d] = (R)(dpv[d] + fc.cen[d] - xc[d]);
+          } else {
+            for (int d = 0; d < D; d++)
+              dri[d] = (D == 3) ? gpr[g1] * fr.t0[d] + gpr[g2] * fr.t1[d] + fr.cen[d] : gpr[g1] * fr.t0[d] + fr.cen[d];
+          }
           R Ui[U];
           for (int u = 0; u < U; u++) {
             R acc = co[u][1] * dri[0];
@@ -634,13 +735,18 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
           R Nb[B];
           Nb[0] = R(1.);
           for (int d = 0; d < D; d++) Nb[1 + d] = dri[d];
-          if (fc.bound == 0) {
+          if (fbound == 0) {
             for (int s1 = 0; s1 < F; s1++) {
               const R aj = P.calph[s1 * nc + nb];
               if (aj == R(0)) continue;
               if (MODE == 2 && s1 == ss) continue;
               R drj[3];
-              for (int d = 0; d < D; d++) drj[d] = (R)(dpv[d] + fc.cen[d] - xn[d]);
+              if constexpr (EX) {
+                for (int d = 0; d < D; d++) drj[d] = (R)(dpv[d] + fc.cen[d] - xn[d]);
+              } else {
+                /* the neighbour centre sits at 2 x the face-centre offset */
+                for (int d = 0; d < D; d++) drj[d] = dri[d] - R(2) * fr.cen[d];
+              }
               R Uj[U];
               for (int u = 0; u < U; u++) {
                 R acc = P.ccoef[((s1 * U + u) * B + 1) * nc + nb] * drj[0];
@@ -739,7 +845,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
                 for (int u = 0; u < U; u++) DFn[b][u] += Fh[u] * Nb[b] * gw * aj;
             }
           } else if (MODE == 2) {
-          } else if (fc.bound == PGDG_BC_WALL) {
+          } else if (fbound == PGDG_BC_WALL) {
             for (int b = 0; b < B; b++) DFn[b][1 + a] += P_i * Nb[b] * gw;
           } else {
             R rho_j = rho_i, P_j = P_i, E_j = E_i;
@@ -748,7 +854,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
               v_j[k] = v_i[k];
               rhov_j[k] = rho_j * v_j[k];
             }
-            if (fc.bound == PGDG_BC_INLET) {
+            if (fbound == PGDG_BC_INLET) {
               rho_j = (R)K.inlet_rho;
               R sqj = R(0);
               for (int k = 0; k < D; k++) {
@@ -759,7 +865,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
               P_j = (R)K.inlet_p;
               E_j = eos_rhoe<R>(P_j, gs, pfe) + R(0.5) * sqj * rho_j;
             }
-            if (fc.bound != PGDG_BC_TRANSMISSIVE) {
+            if (fbound != PGDG_BC_TRANSMISSIVE) {
               if (mirror_j) {
                 v_j[1] = -v_i[1];
                 for (int k = 0; k < D; k++) rhov_j[k] = rho_j * v_j[k];
@@ -793,13 +899,11 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
               for (int u = 0; u < U; u++) DFn[b][u] += Fh[u] * Nb[b] * gw;
           }
         }
-        const R Sj = (R)fc.S;
+        const R Sj = EX ? (R)fc.S : fr.S;
         for (int b = 0; b < B; b++)
           for (int u = 0; u < U; u++) dc[u][b] += (-DFn[b][u] * na) * Sj;
       }
       if constexpr (MODE == 2) continue;
-      const R inv[4] = {R(1. / (voli_d + 1e-20)), R(1. / (mij1 + 1e-20)), R(1. / (mij2 + 1e-20)),
-                        R(1. / (mij3 + 1e-20))};
       for (int u = 0; u < U; u++)
         for (int b = 0; b < B; b++) P.cdcoef[((ss * U + u) * B + b) * nc + ci] = dc[u][b] * inv[b];
     }
@@ -883,7 +987,7 @@ void Launch<D, R, EX>::grid_acc_queued(const CaseK& K, const DevPtrs<R>& P, Ifac
 /* Update_grid (mpm.cpp:768-830)                                      */
 /* ------------------------------------------------------------------ */
 template <int D, typename R, bool EX>
-__global__ void k_update_grid(CaseK K, DevPtrs<R> P, int md) {
+__global__ void __launch_bounds__(256) k_update_grid(CaseK K, DevPtrs<R> P, int md) {
   constexpr int U = D + 2, B = D + 1;
   const int64_t nc = K.ncell;
   const R dt = (R)P.cnt->dt;
@@ -895,42 +999,67 @@ __global__ void k_update_grid(CaseK K, DevPtrs<R> P, int md) {
     R Pc = P.cP[ci];
     for (int s = 0; s < F; s++) {
       R c_s = 0, ac_s = 0;
-      for (int t = 0; t < U; t++) {
-        R l = fabs(P.clim[(s * U + t) * nc + ci]);
-        for (int b = 1; b < B; b++) {
-          int64_t o = ((s * U + t) * B + b) * nc + ci;
-          P.cdcoef[o] *= l;
-          P.ccoef[o] *= l;
+      /* restrict-qualified bases: the loads of later coefficients may run ahead
+       * of the stores of earlier ones */
+      R* __restrict__ cf = P.ccoef + (int64_t)(s * U * B) * nc + ci;
+      R* __restrict__ dcf = P.cdcoef + (int64_t)(s * U * B) * nc + ci;
+      R* __restrict__ c0f = P.ccoef0 + (int64_t)(s * U * B) * nc + ci;
+      const bool present = P.cph[s * nc + ci] == 1;
+      R lim[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) lim[u] = fabs(P.clim[(s * U + u) * nc + ci]);
+      R co0 = R(0), cE = R(0), d00 = R(0), crv[3] = {0, 0, 0}, drv[3] = {0, 0, 0};
+#pragma unroll
+      for (int t = 0; t < U * B; t++) {
+        const int u = t / B, b = t % B;
+        const int64_t o = (int64_t)t * nc;
+        R co = cf[o], d = dcf[o];
+        if (b >= 1) {
+          d *= lim[u];
+          co *= lim[u];
+        }
+        if (present) {
+          if (md == 0) {
+            c0f[o] = co;
+            co = co + d * dt;
+          } else {
+            co = R(0.5) * (d * dt + co + c0f[o]);
+          }
+          dcf[o] = d;
+          cf[o] = co;
+        } else if (b >= 1) {
+          dcf[o] = d;
+          cf[o] = co;
+        }
+        if (b == 0) {
+          if (u == 0) {
+            co0 = co;
+            d00 = d;
+          } else if (u <= D) {
+            crv[u - 1] = co;
+            drv[u - 1] = d;
+          } else {
+            cE = co;
+          }
         }
       }
       const R alph = P.calph[s * nc + ci];
-      if (P.cph[s * nc + ci] == 1) {
-        for (int t = 0; t < U * B; t++) {
-          int64_t o = (s * U * B + t) * nc + ci;
-          R co = P.ccoef[o], d = P.cdcoef[o];
-          if (md == 0) {
-            P.ccoef0[o] = co;
-            P.ccoef[o] = co + d * dt;
-          } else {
-            P.ccoef[o] = R(0.5) * (d * dt + co + P.ccoef0[o]);
-          }
-        }
-        R rho = P.ccoef[((s * U) * B) * nc + ci];
+      if (present) {
+        R rho = co0;
         P.crho[s * nc + ci] = rho;
         R sq = R(0);
         for (int k = 0; k < D; k++) {
-          R rv = P.ccoef[((s * U + 1 + k) * B) * nc + ci];
+          R rv = crv[k];
           P.crhov[(s * D + k) * nc + ci] = rv;
           sq = (k == 0) ? rv * rv : sq + rv * rv;
         }
-        R E = P.ccoef[((s * U + U - 1) * B) * nc + ci];
+        R E = cE;
         P.cE[s * nc + ci] = E;
         Pc = eos_p<R>(E - R(0.5) * sq / rho, (R)K.gamma[s], (R)K.pinf_eos[s]);
         c_s = sqrt_r<R>((R)K.gamma[s] * ((R)K.pinf[s] + Pc) / rho);
-        R d00 = P.cdcoef[((s * U) * B) * nc + ci];
         R asq = R(0);
         for (int k = 0; k < D; k++) {
-          R ak = (P.cdcoef[((s * U + 1 + k) * B) * nc + ci] - d00 * vcur[k]) / rho;
+          R ak = (drv[k] - d00 * vcur[k]) / rho;
           asq = (k == 0) ? ak * ak : asq + ak * ak;
         }
         ac_s = sqrt_r<R>(asq);

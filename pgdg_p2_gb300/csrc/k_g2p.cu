@@ -187,13 +187,13 @@ struct PstSmem {
 };
 
 template <int D, typename R>
-__host__ __device__ inline size_t pst_smem_bytes(int nsc, int nrow, int cap, bool queue = true) {
+__host__ __device__ inline size_t pst_smem_bytes(int nsc, int nrow, int cap, int qdepth = PST_BUF) {
   size_t b = sizeof(int) * (size_t)(3 * nsc + 1);
   b = (b + 31) / 32 * 32;
   b += sizeof(R) * (size_t)(2 * D * nsc);
   b = (b + 31) / 32 * 32;
   b += 4 * sizeof(R) * (size_t)cap;
-  if (queue) b += sizeof(unsigned short) * (size_t)PST_BUF * PST_THREADS;
+  b += sizeof(unsigned short) * (size_t)qdepth * PST_THREADS;
   b += sizeof(R) * (size_t)(4 * nrow);
   b += (size_t)cap;
   return b + 128;
@@ -356,6 +356,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
     if (sm && (lo[d] < sm->lo[d] || hi[d] >= sm->lo[d] + sm->n[d])) inside = false;
   }
   if (inside) {
+    constexpr int BUFV = PST_BUF;
     const R lim2m = pp.lim2 * R(1.0001);
     int nbuf = 0;
     /* sum the queued members in queue (= scan) order */
@@ -383,7 +384,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
       const auto v = sm->ent[e];
       R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
       if (pp.member(xsq)) {
-        if (nbuf == PST_BUF) flush();
+        if (nbuf == BUFV) flush();
         sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
       }
     };
@@ -430,17 +431,17 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
               if (ce < clo || ce > chi) continue;
               R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
               if (pp.member(xsq)) {
-                if constexpr (VAR >= 2) {
+                if constexpr (VAR == 2 || VAR == 3) {
                   pst_rec<D, R, EX>(P, slot_of<R>(v.w), pp); /* summed at once, same order */
                 } else {
-                  if (nbuf == PST_BUF) flush();
+                  if (nbuf == BUFV) flush();
                   sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
                 }
               }
             }
           }
-          if constexpr (VAR < 2)
-            if (__any_sync(__activemask(), nbuf >= PST_BUF / 2)) flush();
+          if constexpr (VAR != 2 && VAR != 3)
+            if (__any_sync(__activemask(), nbuf >= BUFV / 2)) flush();
         }
       } else {
       /* variant 1, warp-cooperative: the lanes walk the union of their
@@ -497,12 +498,12 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
             if (need && ce >= clo && ce <= chi) {
               R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
               if (pp.member(xsq)) {
-                if (nbuf == PST_BUF) flush();
+                if (nbuf == BUFV) flush();
                 sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
               }
             }
           }
-          if (__any_sync(am, nbuf >= PST_BUF / 2)) flush();
+          if (__any_sync(am, nbuf >= BUFV / 2)) flush();
         }
       }
       flush();
@@ -541,7 +542,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
             }
             if (md <= lim2m)
               for (int e = em; e < e1; e++) queue(e);
-            if (__any_sync(__activemask(), nbuf >= PST_BUF / 2)) flush();
+            if (__any_sync(__activemask(), nbuf >= BUFV / 2)) flush();
           }
         }
       flush();
@@ -660,7 +661,7 @@ __global__ void __launch_bounds__(PST_THREADS, (VAR == 3 ? 3 : 2)) k_pst(CaseK K
   sm.ent = reinterpret_cast<V4*>(smem_raw + o);
   sm.buf = reinterpret_cast<unsigned short*>(sm.ent + cap);
   sm.nrow = (D == 3) ? sm.n[0] * sm.n[1] : sm.n[0];
-  sm.rlo = reinterpret_cast<R*>(sm.buf + (VAR >= 2 && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
+  sm.rlo = reinterpret_cast<R*>(sm.buf + ((VAR == 2 || VAR == 3) && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
   sm.rhi = sm.rlo + 2 * sm.nrow;
   sm.ecell = reinterpret_cast<unsigned char*>(sm.rhi + 2 * sm.nrow);
   __shared__ int s_total, s_maxcnt;
@@ -812,15 +813,15 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
   const int nsc = (BK::B0 + 2 * r) * (BK::B1 + 2 * r) * (D == 3 ? BK::B2 + 2 * r : 1);
   const int ppc = (D == 3) ? 8 : 4;
   const int nrow = (D == 3) ? (BK::B0 + 2 * r) * (BK::B1 + 2 * r) : (BK::B0 + 2 * r);
-  const bool queue = EX || VAR < 2;
+  const int qdepth = (!EX && (VAR == 2 || VAR == 3)) ? 0 : PST_BUF;
   /* staging headroom over the nominal count (split children); variant 3 keeps
    * it at 1/8 so three blocks fit in an SM's shared memory */
   int cap = (!EX && VAR == 3) ? nsc * ppc * 9 / 8 : nsc * ppc * 5 / 4;
   if (cap > 65535) cap = 65535;
-  size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, queue);
+  size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, qdepth);
   while (bytes > 220 * 1024 && cap > 256) {
     cap = cap * 3 / 4;
-    bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, queue);
+    bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, qdepth);
   }
   static bool attr_set = false;
   if (!attr_set) {

@@ -598,13 +598,32 @@ __global__ void k_refresh3(CaseK K, DevPtrs<R> P) {
   }
 }
 
-/* mark_in = (x - box_l.x < vol^(1/DIM)) (mpm.cpp:1398-1399) */
+/* mark_in = (x - box_l.x < vol^(1/DIM)) (mpm.cpp:1398-1399).  events (may be
+ * NULL): the event count of the merge pass just run; with no merge nothing
+ * mark_in depends on has changed since the last evaluation and the kernel
+ * returns at once.  The FP32 path decides in FP32 when x - box_l is more than
+ * 0.1% away from vol^(1/DIM) (far beyond the rounding of either side) and
+ * evaluates the rest exactly, as the FP64 path does. */
 template <int D, typename R>
-__global__ void k_mark_in(CaseK K, DevPtrs<R> P) {
+__global__ void k_mark_in(CaseK K, DevPtrs<R> P, const unsigned long long* events) {
+  if (events && *events == 0) return;
   const int64_t n = (int64_t)P.cnt->n_slots;
   const R* X = P.X[P.xb];
+  const float blf = (float)K.bl[0];
   GRID_STRIDE(p, n) {
     if (P.phase[p] == 0) continue;
+    if constexpr (sizeof(R) == 4) {
+      const float af = (float)X[p] - blf;
+      const float rf = (D == 2) ? sqrtf((float)P.vol[p]) : cbrtf((float)P.vol[p]);
+      if (af > rf * 1.001f) {
+        P.mark_in[p] = 0;
+        continue;
+      }
+      if (af < rf * 0.999f) {
+        P.mark_in[p] = 1;
+        continue;
+      }
+    }
     double a = dsub((double)X[p], K.bl[0]);
     double vol = (double)P.vol[p];
     double ra = (D == 2) ? sqrt(vol) : cbrt(vol);
@@ -633,7 +652,7 @@ void Launch<D, R, EX>::split(const CaseK& K, const DevPtrs<R>& P, cudaStream_t s
   k_bucket_fix<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P, 0);
   k_aff_cells<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P);
   k_refresh3<D, R><<<g, BLK, 0, st>>>(K, P);
-  k_mark_in<D, R><<<g, BLK, 0, st>>>(K, P);
+  k_mark_in<D, R><<<g, BLK, 0, st>>>(K, P, nullptr);
   k_reset_queues<R><<<1, 1, 0, st>>>(P);
 }
 
@@ -780,7 +799,8 @@ void Launch<D, R, EX>::merge(const CaseK& K, const DevPtrs<R>& P, cudaStream_t s
   k_bucket_fix<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P, 0);
   k_aff_cells<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P);
   k_refresh3<D, R><<<g, BLK, 0, st>>>(K, P);
-  k_mark_in<D, R><<<g, BLK, 0, st>>>(K, P);
+  /* the pass's merge count is still the scan total */
+  k_mark_in<D, R><<<g, BLK, 0, st>>>(K, P, P.scan_blk + scan_nblk(K.cap));
   k_reset_queues<R><<<1, 1, 0, st>>>(P);
 }
 

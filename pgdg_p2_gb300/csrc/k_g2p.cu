@@ -10,6 +10,8 @@
  * which is recomputed on the fly from the stage-start coordinate buffer instead
  * of being stored.
  */
+#include <type_traits>
+
 #include "pgdg_dev.cuh"
 
 namespace pgdg {
@@ -153,6 +155,22 @@ template <>
 struct Brick<2> {
   static constexpr int B0 = 8, B1 = 8, B2 = 1;
 };
+/* the larger brick of variant 5: twice the cells, 512 threads, a smaller
+ * staged halo per particle */
+template <int D>
+struct BigBrick;
+template <>
+struct BigBrick<3> {
+  static constexpr int B0 = 4, B1 = 4, B2 = 4;
+};
+template <>
+struct BigBrick<2> {
+  static constexpr int B0 = 16, B1 = 8, B2 = 1;
+};
+template <int D, int VAR>
+using BrickOf = typename std::conditional<VAR == 5, BigBrick<D>, Brick<D>>::type;
+__host__ __device__ constexpr int pst_threads(int var) { return var == 5 ? 512 : 256; }
+__host__ __device__ constexpr int pst_minblocks(int var) { return var == 3 ? 3 : 2; }
 constexpr int PST_THREADS = 256;
 constexpr int PST_BUF = 64;
 
@@ -431,7 +449,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
               if (ce < clo || ce > chi) continue;
               R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
               if (pp.member(xsq)) {
-                if constexpr (VAR == 2 || VAR == 3) {
+                if constexpr (VAR == 2 || VAR == 3 || VAR == 5) {
                   pst_rec<D, R, EX>(P, slot_of<R>(v.w), pp); /* summed at once, same order */
                 } else {
                   if (nbuf == BUFV) flush();
@@ -440,7 +458,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
               }
             }
           }
-          if constexpr (VAR != 2 && VAR != 3)
+          if constexpr (VAR == 0)
             if (__any_sync(__activemask(), nbuf >= BUFV / 2)) flush();
         }
       } else {
@@ -620,9 +638,9 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
 }
 
 template <int D, typename R, bool EX, int VAR>
-__global__ void __launch_bounds__(PST_THREADS, (VAR == 3 ? 3 : 2)) k_pst(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn,
+__global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn,
                                                     int nb0, int nb1, int cap) {
-  using BK = Brick<D>;
+  using BK = BrickOf<D, VAR>;
   using V4 = typename Vec4<R>::T;
   extern __shared__ __align__(32) unsigned char smem_raw[];
   const R dt = (R)P.cnt->dt;
@@ -661,7 +679,7 @@ __global__ void __launch_bounds__(PST_THREADS, (VAR == 3 ? 3 : 2)) k_pst(CaseK K
   sm.ent = reinterpret_cast<V4*>(smem_raw + o);
   sm.buf = reinterpret_cast<unsigned short*>(sm.ent + cap);
   sm.nrow = (D == 3) ? sm.n[0] * sm.n[1] : sm.n[0];
-  sm.rlo = reinterpret_cast<R*>(sm.buf + ((VAR == 2 || VAR == 3) && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
+  sm.rlo = reinterpret_cast<R*>(sm.buf + ((VAR == 2 || VAR == 3 || VAR == 5) && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
   sm.rhi = sm.rlo + 2 * sm.nrow;
   sm.ecell = reinterpret_cast<unsigned char*>(sm.rhi + 2 * sm.nrow);
   __shared__ int s_total, s_maxcnt;
@@ -805,7 +823,7 @@ __global__ void __launch_bounds__(PST_THREADS, (VAR == 3 ? 3 : 2)) k_pst(CaseK K
 
 template <int D, typename R, bool EX, int VAR>
 static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, cudaStream_t st) {
-  using BK = Brick<D>;
+  using BK = BrickOf<D, VAR>;
   const int nb0 = (D == 3) ? (K.N[2] + BK::B2 - 1) / BK::B2 : 1;
   const int nb1 = (K.N[1] + BK::B1 - 1) / BK::B1;
   const int nbx = (K.N[0] + BK::B0 - 1) / BK::B0;
@@ -813,10 +831,10 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
   const int nsc = (BK::B0 + 2 * r) * (BK::B1 + 2 * r) * (D == 3 ? BK::B2 + 2 * r : 1);
   const int ppc = (D == 3) ? 8 : 4;
   const int nrow = (D == 3) ? (BK::B0 + 2 * r) * (BK::B1 + 2 * r) : (BK::B0 + 2 * r);
-  const int qdepth = (!EX && (VAR == 2 || VAR == 3)) ? 0 : PST_BUF;
+  const int qdepth = (!EX && (VAR == 2 || VAR == 3 || VAR == 5)) ? 0 : PST_BUF;
   /* staging headroom over the nominal count (split children); variant 3 keeps
    * it at 1/8 so three blocks fit in an SM's shared memory */
-  int cap = (!EX && VAR == 3) ? nsc * ppc * 9 / 8 : nsc * ppc * 5 / 4;
+  int cap = (!EX && (VAR == 3 || VAR == 5)) ? nsc * ppc * 9 / 8 : nsc * ppc * 5 / 4;
   if (cap > 65535) cap = 65535;
   size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, qdepth);
   while (bytes > 220 * 1024 && cap > 256) {
@@ -828,16 +846,17 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
     cudaFuncSetAttribute(k_pst<D, R, EX, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 224 * 1024);
     attr_set = true;
   }
-  k_pst<D, R, EX, VAR><<<nbx * nb1 * nb0, PST_THREADS, bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap);
+  k_pst<D, R, EX, VAR><<<nbx * nb1 * nb0, pst_threads(VAR), bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap);
 }
 
 /* variants of the shifting kernel (identical results; the context's autotuner
  * times them on its own state and keeps the fastest): 0 per-lane row scan with
  * queued members, 1 warp-cooperative row scan, 2 per-lane scan summing members
- * at once, 3 the same for 3 blocks per SM.  The exact path has one. */
+ * at once, 3 the same for 3 blocks per SM, 4 direct sums over bricks of twice
+ * the cells with 512 threads.  The exact path has one. */
 template <int D, typename R, bool EX>
 int Launch<D, R, EX>::pst_variants() {
-  return EX ? 1 : 4;
+  return EX ? 1 : 5;
 }
 
 template <int D, typename R, bool EX>
@@ -849,6 +868,7 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
     if (var == 1) pst_launch<D, R, EX, 1>(K, P, xs, hs, xn, hn, st);
     else if (var == 2) pst_launch<D, R, EX, 2>(K, P, xs, hs, xn, hn, st);
     else if (var == 3) pst_launch<D, R, EX, 3>(K, P, xs, hs, xn, hn, st);
+    else if (var == 4) pst_launch<D, R, EX, 5>(K, P, xs, hs, xn, hn, st);
     else pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, st);
   }
 }

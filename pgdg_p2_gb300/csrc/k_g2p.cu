@@ -167,10 +167,24 @@ template <>
 struct BigBrick<2> {
   static constexpr int B0 = 16, B1 = 8, B2 = 1;
 };
+/* and the largest brick of variant 6: four times the cells, 1024 threads, one
+ * block per SM */
+template <int D>
+struct HugeBrick;
+template <>
+struct HugeBrick<3> {
+  static constexpr int B0 = 4, B1 = 4, B2 = 8;
+};
+template <>
+struct HugeBrick<2> {
+  static constexpr int B0 = 16, B1 = 16, B2 = 1;
+};
 template <int D, int VAR>
-using BrickOf = typename std::conditional<VAR == 5, BigBrick<D>, Brick<D>>::type;
-__host__ __device__ constexpr int pst_threads(int var) { return var == 5 ? 512 : 256; }
-__host__ __device__ constexpr int pst_minblocks(int var) { return var == 3 ? 3 : 2; }
+using BrickOf = typename std::conditional<VAR == 6, HugeBrick<D>,
+                                          typename std::conditional<VAR == 5, BigBrick<D>, Brick<D>>::type>::type;
+__host__ __device__ constexpr int pst_threads(int var) { return var == 6 ? 1024 : var == 5 ? 512 : 256; }
+__host__ __device__ constexpr int pst_minblocks(int var) { return var == 3 ? 3 : var == 6 ? 1 : 2; }
+__host__ __device__ constexpr bool pst_direct(int var) { return var == 2 || var == 3 || var == 5 || var == 6; }
 constexpr int PST_THREADS = 256;
 constexpr int PST_BUF = 64;
 
@@ -449,7 +463,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
               if (ce < clo || ce > chi) continue;
               R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
               if (pp.member(xsq)) {
-                if constexpr (VAR == 2 || VAR == 3 || VAR == 5) {
+                if constexpr (pst_direct(VAR)) {
                   pst_rec<D, R, EX>(P, slot_of<R>(v.w), pp); /* summed at once, same order */
                 } else {
                   if (nbuf == BUFV) flush();
@@ -679,7 +693,7 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
   sm.ent = reinterpret_cast<V4*>(smem_raw + o);
   sm.buf = reinterpret_cast<unsigned short*>(sm.ent + cap);
   sm.nrow = (D == 3) ? sm.n[0] * sm.n[1] : sm.n[0];
-  sm.rlo = reinterpret_cast<R*>(sm.buf + ((VAR == 2 || VAR == 3 || VAR == 5) && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
+  sm.rlo = reinterpret_cast<R*>(sm.buf + (pst_direct(VAR) && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
   sm.rhi = sm.rlo + 2 * sm.nrow;
   sm.ecell = reinterpret_cast<unsigned char*>(sm.rhi + 2 * sm.nrow);
   __shared__ int s_total, s_maxcnt;
@@ -831,10 +845,10 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
   const int nsc = (BK::B0 + 2 * r) * (BK::B1 + 2 * r) * (D == 3 ? BK::B2 + 2 * r : 1);
   const int ppc = (D == 3) ? 8 : 4;
   const int nrow = (D == 3) ? (BK::B0 + 2 * r) * (BK::B1 + 2 * r) : (BK::B0 + 2 * r);
-  const int qdepth = (!EX && (VAR == 2 || VAR == 3 || VAR == 5)) ? 0 : PST_BUF;
+  const int qdepth = (!EX && pst_direct(VAR)) ? 0 : PST_BUF;
   /* staging headroom over the nominal count (split children); variant 3 keeps
    * it at 1/8 so three blocks fit in an SM's shared memory */
-  int cap = (!EX && (VAR == 3 || VAR == 5)) ? nsc * ppc * 9 / 8 : nsc * ppc * 5 / 4;
+  int cap = (!EX && (VAR == 3 || VAR >= 5)) ? nsc * ppc * 9 / 8 : nsc * ppc * 5 / 4;
   if (cap > 65535) cap = 65535;
   size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, qdepth);
   while (bytes > 220 * 1024 && cap > 256) {
@@ -853,10 +867,11 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
  * times them on its own state and keeps the fastest): 0 per-lane row scan with
  * queued members, 1 warp-cooperative row scan, 2 per-lane scan summing members
  * at once, 3 the same for 3 blocks per SM, 4 direct sums over bricks of twice
- * the cells with 512 threads.  The exact path has one. */
+ * the cells with 512 threads, 5 over bricks of four times the cells with 1024
+ * threads.  The exact path has one. */
 template <int D, typename R, bool EX>
 int Launch<D, R, EX>::pst_variants() {
-  return EX ? 1 : 5;
+  return EX ? 1 : 6;
 }
 
 template <int D, typename R, bool EX>
@@ -869,6 +884,7 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
     else if (var == 2) pst_launch<D, R, EX, 2>(K, P, xs, hs, xn, hn, st);
     else if (var == 3) pst_launch<D, R, EX, 3>(K, P, xs, hs, xn, hn, st);
     else if (var == 4) pst_launch<D, R, EX, 5>(K, P, xs, hs, xn, hn, st);
+    else if (var == 5) pst_launch<D, R, EX, 6>(K, P, xs, hs, xn, hn, st);
     else pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, st);
   }
 }

@@ -131,6 +131,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def pinned_alloc():
+    """Array allocator in page-locked host memory (through torch's pinned
+    allocator; the arrays keep their buffers alive)."""
+    import numpy as np
+    import torch
+
+    def alloc(shape, dtype):
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        t = torch.empty(max(nbytes, 1), dtype=torch.uint8, pin_memory=True)
+        return t.numpy()[:nbytes].view(dtype).reshape(shape)
+    return alloc
+
+
 def state_bytes(p, c):
     tot = 0
     for a in p.as_dict().values():
@@ -205,22 +218,37 @@ def run_ours(args):
         g.close()
         return
 
-    # ---- end to end through the C ABI with host buffers ----
+    # ---- end to end through the C ABI with host buffers in page-locked memory ----
     g2 = M.MPM(cs, PREC_MIXED)
     g2.set_surrogate(net)
     ke = args.steps
-    nbytes = state_bytes(p, c)
+    pin = pinned_alloc()
+    ph, ch = M.Particles(p.n, cs.dim, alloc=pin), M.Cells(ncell, cs.dim, alloc=pin)
+    for k in ph.NAMES:
+        getattr(ph, k)[...] = getattr(p, k)
+    for k in ch.NAMES:
+        getattr(ch, k)[...] = getattr(c, k)
+    q = M.Particles(p.n + p.n // 4, cs.dim, alloc=pin)
+    cq = M.Cells(ncell, cs.dim, alloc=pin)
+    nbytes = state_bytes(ph, ch)
+    # warm-up of this context (kernel-variant tuning, first-use buffers), then
+    # the timed region starts again from the host state
+    g2.upload_particles(ph)
+    g2.upload_cells(ch)
+    g2.advance(args.warmup)
+    g2.sync()
     t0 = time.perf_counter()
-    g2.upload_particles(p)
-    g2.upload_cells(c)
+    g2.upload_particles(ph)
+    g2.upload_cells(ch)
     for _ in range(ke):
         g2.advance(1)
         g2.stats()                 # device->host read of dt / max_v / counters
-    q = g2.download_particles()
-    cq = g2.download_cells()
+    g2.download_particles(out=q)
+    g2.download_cells(out=cq)
     g2.sync()
     te = time.perf_counter() - t0
-    dbytes = state_bytes(q, cq)
+    dbytes = (sum(a.nbytes for a in q.as_dict().values()) * q.n // max(q.cap, 1)
+              + sum(a.nbytes for a in cq.as_dict().values()))
     e2e = {"value": ws * ncell * 2 * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes // ke,
            "d2h_bytes_per_step": dbytes // ke + 160, "steps": ke, "seconds": te}
     g2.close()

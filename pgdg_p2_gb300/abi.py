@@ -124,25 +124,27 @@ PARTICLE_FIELDS = {
 
 
 class Particles:
-    """numpy SoA of fluid particles (canonical order)."""
+    """numpy arrays of fluid particles (canonical order).  alloc(shape, dtype)
+    may supply the arrays (e.g. page-locked host memory); default np.zeros."""
 
-    def __init__(self, n, dim):
+    def __init__(self, n, dim, alloc=None):
+        z = alloc or np.zeros
         self.dim = dim
         self.cap = int(n)
         self.n = int(n)
         U = dim + 2
         ns = U * dim
         f8 = np.float64
-        self.coord = np.zeros((n, 3), f8)
-        self.v = np.zeros((n, 3), f8)
-        self.tv = np.zeros((n, 3), f8)
-        self.rhov = np.zeros((n, 3), f8)
+        self.coord = z((n, 3), f8)
+        self.v = z((n, 3), f8)
+        self.tv = z((n, 3), f8)
+        self.rhov = z((n, 3), f8)
         for k in ("vol", "mass", "h", "P", "rho", "E", "c"):
-            setattr(self, k, np.zeros(n, f8))
-        self.slope = np.zeros((n, ns), f8)
-        self.phase = np.zeros(n, np.int32)
-        self.mark_in = np.zeros(n, np.int32)
-        self.seq = np.zeros(n, np.uint64)
+            setattr(self, k, z((n,), f8))
+        self.slope = z((n, ns), f8)
+        self.phase = z((n,), np.int32)
+        self.mark_in = z((n,), np.int32)
+        self.seq = z((n,), np.uint64)
 
     NAMES = ("coord", "v", "tv", "rhov", "vol", "mass", "h", "P", "rho", "E", "c", "slope",
              "phase", "mark_in", "seq")
@@ -179,26 +181,27 @@ class Cells:
     NAMES = ("rho", "rhov", "E", "c", "ac", "alph", "coef", "v", "P", "ph_state", "ph_state_b",
              "used", "lim_u", "g_v", "dcoef")
 
-    def __init__(self, n, dim):
+    def __init__(self, n, dim, alloc=None):
+        z = alloc or np.zeros
         self.dim = dim
         self.n = int(n)
         U, B = dim + 2, dim + 1
         f8 = np.float64
-        self.rho = np.zeros((n, F), f8)
-        self.rhov = np.zeros((n, F, 3), f8)
-        self.E = np.zeros((n, F), f8)
-        self.c = np.zeros((n, F), f8)
-        self.ac = np.zeros((n, F), f8)
-        self.alph = np.zeros((n, F), f8)
-        self.coef = np.zeros((n, F, U, B), f8)
-        self.v = np.zeros((n, 3), f8)
-        self.P = np.zeros(n, f8)
-        self.ph_state = np.zeros((n, F), np.int32)
-        self.ph_state_b = np.zeros((n, F), np.int32)
-        self.used = np.zeros(n, np.int32)
-        self.lim_u = np.zeros((n, F, U), f8)
-        self.g_v = np.zeros((n, dim, dim), f8)
-        self.dcoef = np.zeros((n, F, U, B), f8)
+        self.rho = z((n, F), f8)
+        self.rhov = z((n, F, 3), f8)
+        self.E = z((n, F), f8)
+        self.c = z((n, F), f8)
+        self.ac = z((n, F), f8)
+        self.alph = z((n, F), f8)
+        self.coef = z((n, F, U, B), f8)
+        self.v = z((n, 3), f8)
+        self.P = z((n,), f8)
+        self.ph_state = z((n, F), np.int32)
+        self.ph_state_b = z((n, F), np.int32)
+        self.used = z((n,), np.int32)
+        self.lim_u = z((n, F, U), f8)
+        self.g_v = z((n, dim, dim), f8)
+        self.dcoef = z((n, F, U, B), f8)
 
     def view(self):
         s = pgdg_cells()

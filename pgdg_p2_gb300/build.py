@@ -26,6 +26,7 @@ CU = [("k_particles.cu", "k_particles", ["-fmad=false"]),
       ("k_g2p.cu", "k_g2p_x", ["-fmad=false", "-DPGDG_EXACT_TU"]),
       ("k_mgfm.cu", "k_mgfm", ["-fmad=false"]),
       ("k_mlp.cu", "k_mlp", ["-fmad=false"]),
+      ("k_xfer.cu", "k_xfer", []),
       ("capi.cu", "capi", [])]
 CPP = ["case_builder.cpp"]
 

@@ -362,60 +362,82 @@ struct Ctx : pgdg_ctx {
   }
 
   /* ---------------- exchange ---------------- */
+  /* staging buffer of the host exchange (raw host chunks; allocated on first use) */
+  XferStage stage{nullptr, 0};
+  int64_t* d_alive = nullptr;
+  int ensure_stage() {
+    if (stage.buf) return PGDG_OK;
+    stage.bytes = (size_t)256 << 20;
+    CK(cudaMalloc(&stage.buf, stage.bytes));
+    allocs.push_back(stage.buf);
+    return PGDG_OK;
+  }
+  /* live slots in canonical order into d_alive; returns their number */
+  int alive(int64_t* n) {
+    if (!d_alive) CK(A(&d_alive, (size_t)K.cap));
+    alive_index(P.phase, P.scan, P.scan_blk, &P.cnt->n_slots, K.cap, d_alive, st);
+    unsigned long long tot = 0;
+    CK(cudaMemcpyAsync(&tot, P.scan_blk + scan_nblk_host(K.cap), sizeof(tot), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *n = (int64_t)tot;
+    return PGDG_OK;
+  }
+  static int scan_nblk_host(int64_t cap) { return (int)((cap + 2047) / 2048); }
+
+  /* ---------------- exchange ---------------- */
   int upload_particles(const pgdg_particles* pp) override {
     int64_t n = pp->n;
     if (n > K.cap) {
       err = "particle count exceeds capacity";
       return PGDG_EINVAL;
     }
-    std::vector<R> x(D * n), v(D * n), tv(D * n), rhov(D * n), sl(NS * n);
-    std::vector<R> vol(n), mass(n), h(n), Pp(n), rho(n), E(n), c(n);
-    std::vector<int8_t> phase(n), mark(n);
-    std::vector<uint64_t> seq(n);
-    std::vector<int32_t> llen(n, 0);
-    std::vector<int64_t> loff(n, 0);
-    uint64_t mx = 0;
-    for (int64_t i = 0; i < n; i++) {
-      for (int d = 0; d < D; d++) {
-        x[d * n + i] = (R)pp->coord[3 * i + d];
-        v[d * n + i] = pp->v ? (R)pp->v[3 * i + d] : R(0);
-        tv[d * n + i] = pp->tv ? (R)pp->tv[3 * i + d] : R(0);
-        rhov[d * n + i] = (R)pp->rhov[3 * i + d];
-      }
-      vol[i] = (R)pp->vol[i]; mass[i] = (R)pp->mass[i]; h[i] = (R)pp->h[i]; Pp[i] = (R)pp->P[i];
-      rho[i] = (R)pp->rho[i]; c[i] = (R)pp->c[i];
-      {
-        const int s = pp->phase[i] - 1;
-        E[i] = (R)(s >= 0 && s < F && K.eshift[s] != 0.0 ? pp->E[i] - K.eshift[s] : pp->E[i]);
-      }
-      for (int t = 0; t < NS; t++) sl[t * n + i] = pp->slope ? (R)pp->slope[NS * i + t] : R(0);
-      phase[i] = (int8_t)pp->phase[i];
-      mark[i] = pp->mark_in ? (int8_t)pp->mark_in[i] : 0;
-      seq[i] = pp->seq ? pp->seq[i] : (uint64_t)i;
-      mx = std::max<uint64_t>(mx, seq[i] + 1);
+    if (!pp->coord || !pp->rhov || !pp->vol || !pp->mass || !pp->h || !pp->P || !pp->rho || !pp->E || !pp->c ||
+        !pp->phase) {
+      err = "upload_particles: a required array is NULL";
+      return PGDG_EINVAL;
     }
-    auto put = [&](R* dst, const std::vector<R>& src, int comps) -> cudaError_t {
-      for (int k = 0; k < comps; k++) {
-        cudaError_t e = cudaMemcpy(dst + (size_t)k * K.cap, src.data() + (size_t)k * n, sizeof(R) * n,
-                                   cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return e;
-      }
-      return cudaSuccess;
-    };
+    int rc = ensure_stage();
+    if (rc) return rc;
     CK(cudaStreamSynchronize(st));
     P.xb = 0;
     P.hb = 0;
     x0b = 0;
-    CK(put(P.X[0], x, D)); CK(put(P.v, v, D)); CK(put(P.tv, tv, D)); CK(put(P.rhov, rhov, D));
-    CK(put(P.sl, sl, NS));
-    CK(put(P.vol, vol, 1)); CK(put(P.mass, mass, 1)); CK(put(P.H[0], h, 1)); CK(put(P.P, Pp, 1));
-    CK(put(P.rho, rho, 1)); CK(put(P.E, E, 1)); CK(put(P.c, c, 1));
-    CK(cudaMemset(P.phase, 0, K.cap));
-    CK(cudaMemcpy(P.phase, phase.data(), n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.mark_in, mark.data(), n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.seq, seq.data(), 8 * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.list_len, llen.data(), 4 * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.list_off, loff.data(), 8 * n, cudaMemcpyHostToDevice));
+    const int64_t cap = K.cap;
+    const XferMap vec = xmap(D), one = xmap(1), sl = xmap(NS);
+    /* phase first: the energy shift of a particle follows its phase */
+    CK(cudaMemsetAsync(P.phase, 0, (size_t)cap, st));
+    CK(xfer_h2d_i8(pp->phase, 1, n, one, P.phase, cap, stage, st));
+    CK(xfer_h2d<R>(pp->coord, 3, n, vec, P.X[0], cap, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(pp->rhov, 3, n, vec, P.rhov, cap, nullptr, nullptr, stage, st));
+    for (int d = 0; d < D; d++) {
+      if (!pp->v) CK(cudaMemsetAsync(P.v + (size_t)d * cap, 0, sizeof(R) * n, st));
+      if (!pp->tv) CK(cudaMemsetAsync(P.tv + (size_t)d * cap, 0, sizeof(R) * n, st));
+    }
+    if (pp->v) CK(xfer_h2d<R>(pp->v, 3, n, vec, P.v, cap, nullptr, nullptr, stage, st));
+    if (pp->tv) CK(xfer_h2d<R>(pp->tv, 3, n, vec, P.tv, cap, nullptr, nullptr, stage, st));
+    if (pp->slope) CK(xfer_h2d<R>(pp->slope, NS, n, sl, P.sl, cap, nullptr, nullptr, stage, st));
+    else
+      for (int t = 0; t < NS; t++) CK(cudaMemsetAsync(P.sl + (size_t)t * cap, 0, sizeof(R) * n, st));
+    CK(xfer_h2d<R>(pp->vol, 1, n, one, P.vol, cap, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(pp->mass, 1, n, one, P.mass, cap, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(pp->h, 1, n, one, P.H[0], cap, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(pp->P, 1, n, one, P.P, cap, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(pp->rho, 1, n, one, P.rho, cap, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(pp->E, 1, n, one, P.E, cap, P.phase, K.eshift, stage, st));
+    CK(xfer_h2d<R>(pp->c, 1, n, one, P.c, cap, nullptr, nullptr, stage, st));
+    if (pp->mark_in) CK(xfer_h2d_i8(pp->mark_in, 1, n, one, P.mark_in, cap, stage, st));
+    else CK(cudaMemsetAsync(P.mark_in, 0, (size_t)n, st));
+    uint64_t mx = (uint64_t)n;
+    if (pp->seq) {
+      CK(cudaMemcpyAsync(P.seq, pp->seq, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
+      mx = 0;
+      for (int64_t i = 0; i < n; i++) mx = std::max<uint64_t>(mx, pp->seq[i] + 1);
+    } else {
+      iota_u64(P.seq, n, st);
+    }
+    CK(cudaMemsetAsync(P.list_len, 0, sizeof(int32_t) * n, st));
+    CK(cudaMemsetAsync(P.list_off, 0, sizeof(int64_t) * n, st));
+    CK(cudaStreamSynchronize(st));
     DevCounters hc = counters();
     hc.n_slots = n;
     hc.n_live = n;
@@ -427,15 +449,13 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
 
-  /* alive slots in canonical order */
+  /* alive slots in canonical order (host copy, for the list exchange) */
   int alive_slots(std::vector<int64_t>& slots) {
-    DevCounters hc = counters();
-    int64_t ns = (int64_t)hc.n_slots;
-    std::vector<int8_t> ph(ns);
-    if (ns) CK(cudaMemcpy(ph.data(), P.phase, ns, cudaMemcpyDeviceToHost));
-    slots.clear();
-    for (int64_t s = 0; s < ns; s++)
-      if (ph[s] != 0) slots.push_back(s);
+    int64_t n = 0;
+    int rc = alive(&n);
+    if (rc) return rc;
+    slots.resize(n);
+    if (n) CK(cudaMemcpy(slots.data(), d_alive, sizeof(int64_t) * n, cudaMemcpyDeviceToHost));
     return PGDG_OK;
   }
 
@@ -446,113 +466,88 @@ struct Ctx : pgdg_ctx {
   }
 
   int download_particles(pgdg_particles* pp) override {
-    std::vector<int64_t> slots;
-    int rc = alive_slots(slots);
+    int rc = ensure_stage();
     if (rc) return rc;
-    int64_t n = (int64_t)slots.size();
+    int64_t n = 0;
+    rc = alive(&n);
+    if (rc) return rc;
     if (pp->n < n) {
       pp->n = n;
       err = "download capacity too small";
       return PGDG_EINVAL;
     }
-    DevCounters hc = counters();
-    int64_t ns = (int64_t)hc.n_slots;
-    auto get = [&](const R* src, int comps, std::vector<R>& dst) -> cudaError_t {
-      dst.resize((size_t)comps * std::max<int64_t>(ns, 1));
-      for (int k = 0; k < comps; k++) {
-        cudaError_t e = cudaMemcpy(dst.data() + (size_t)k * ns, src + (size_t)k * K.cap, sizeof(R) * ns,
-                                   cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return e;
-      }
-      return cudaSuccess;
-    };
-    std::vector<R> x, v, tv, rhov, sl, vol, mass, h, Pp, rho, E, c;
-    CK(get(P.X[P.xb], D, x)); CK(get(P.v, D, v)); CK(get(P.tv, D, tv)); CK(get(P.rhov, D, rhov));
-    CK(get(P.sl, NS, sl)); CK(get(P.vol, 1, vol)); CK(get(P.mass, 1, mass)); CK(get(P.H[P.hb], 1, h));
-    CK(get(P.P, 1, Pp)); CK(get(P.rho, 1, rho)); CK(get(P.E, 1, E)); CK(get(P.c, 1, c));
-    std::vector<int8_t> phase(std::max<int64_t>(ns, 1)), mark(std::max<int64_t>(ns, 1));
-    std::vector<uint64_t> seq(std::max<int64_t>(ns, 1));
-    CK(cudaMemcpy(phase.data(), P.phase, ns, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(mark.data(), P.mark_in, ns, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(seq.data(), P.seq, 8 * ns, cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < n; i++) {
-      int64_t s = slots[i];
-      for (int d = 0; d < 3; d++) {
-        bool in = d < D;
-        if (pp->coord) pp->coord[3 * i + d] = in ? (double)x[d * ns + s] : 0.0;
-        if (pp->v) pp->v[3 * i + d] = in ? (double)v[d * ns + s] : 0.0;
-        if (pp->tv) pp->tv[3 * i + d] = in ? (double)tv[d * ns + s] : 0.0;
-        if (pp->rhov) pp->rhov[3 * i + d] = in ? (double)rhov[d * ns + s] : 0.0;
-      }
-      if (pp->vol) pp->vol[i] = vol[s];
-      if (pp->mass) pp->mass[i] = mass[s];
-      if (pp->h) pp->h[i] = h[s];
-      if (pp->P) pp->P[i] = Pp[s];
-      if (pp->rho) pp->rho[i] = rho[s];
-      if (pp->E) {
-        const int f = phase[s] - 1;
-        pp->E[i] = (f >= 0 && f < F && K.eshift[f] != 0.0) ? (double)E[s] + K.eshift[f] : (double)E[s];
-      }
-      if (pp->c) pp->c[i] = c[s];
-      if (pp->slope)
-        for (int t = 0; t < NS; t++) pp->slope[NS * i + t] = sl[t * ns + s];
-      if (pp->phase) pp->phase[i] = phase[s];
-      if (pp->mark_in) pp->mark_in[i] = mark[s];
-      if (pp->seq) pp->seq[i] = seq[s];
-    }
+    const int64_t cap = K.cap;
+    const int64_t* ix = d_alive;
+    const XferMap vec = xmap(D), one = xmap(1), sl = xmap(NS);
+    if (pp->coord) CK(xfer_d2h<R>(P.X[P.xb], cap, ix, n, vec, pp->coord, 3, nullptr, nullptr, stage, st));
+    if (pp->v) CK(xfer_d2h<R>(P.v, cap, ix, n, vec, pp->v, 3, nullptr, nullptr, stage, st));
+    if (pp->tv) CK(xfer_d2h<R>(P.tv, cap, ix, n, vec, pp->tv, 3, nullptr, nullptr, stage, st));
+    if (pp->rhov) CK(xfer_d2h<R>(P.rhov, cap, ix, n, vec, pp->rhov, 3, nullptr, nullptr, stage, st));
+    if (pp->slope) CK(xfer_d2h<R>(P.sl, cap, ix, n, sl, pp->slope, NS, nullptr, nullptr, stage, st));
+    if (pp->vol) CK(xfer_d2h<R>(P.vol, cap, ix, n, one, pp->vol, 1, nullptr, nullptr, stage, st));
+    if (pp->mass) CK(xfer_d2h<R>(P.mass, cap, ix, n, one, pp->mass, 1, nullptr, nullptr, stage, st));
+    if (pp->h) CK(xfer_d2h<R>(P.H[P.hb], cap, ix, n, one, pp->h, 1, nullptr, nullptr, stage, st));
+    if (pp->P) CK(xfer_d2h<R>(P.P, cap, ix, n, one, pp->P, 1, nullptr, nullptr, stage, st));
+    if (pp->rho) CK(xfer_d2h<R>(P.rho, cap, ix, n, one, pp->rho, 1, nullptr, nullptr, stage, st));
+    if (pp->E) CK(xfer_d2h<R>(P.E, cap, ix, n, one, pp->E, 1, P.phase, K.eshift, stage, st));
+    if (pp->c) CK(xfer_d2h<R>(P.c, cap, ix, n, one, pp->c, 1, nullptr, nullptr, stage, st));
+    if (pp->phase) CK(xfer_d2h_i8(P.phase, cap, ix, n, one, pp->phase, 1, stage, st));
+    if (pp->mark_in) CK(xfer_d2h_i8(P.mark_in, cap, ix, n, one, pp->mark_in, 1, stage, st));
+    if (pp->seq) CK(xfer_d2h_u64(P.seq, ix, n, pp->seq, stage, st));
     pp->n = n;
     return PGDG_OK;
   }
 
+  /* cell arrays: host element = cell, device component-major over ncell */
   int upload_cells(const pgdg_cells* cc) override {
     if (cc->n != K.ncell) {
       err = "cell count mismatch";
       return PGDG_EINVAL;
     }
-    const int64_t nc = K.ncell;
-    std::vector<R> rho(F * nc), rhov(F * D * nc), E(F * nc), c(F * nc), ac(F * nc), alph(F * nc),
-        coef(F * U * B * nc), lim(F * U * nc), gv(D * D * nc), v(D * nc), Pp(nc), dco(F * U * B * nc);
-    std::vector<int8_t> ph(F * nc), phb(F * nc), used(nc);
-    for (int64_t ci = 0; ci < nc; ci++) {
-      for (int s = 0; s < F; s++) {
-        int64_t q = ci * F + s;
-        rho[s * nc + ci] = (R)cc->rho[q];
-        for (int d = 0; d < D; d++) rhov[(s * D + d) * nc + ci] = (R)cc->rhov[q * 3 + d];
-        E[s * nc + ci] = (R)(K.eshift[s] != 0.0 ? cc->E[q] - K.eshift[s] : cc->E[q]);
-        c[s * nc + ci] = (R)cc->c[q];
-        ac[s * nc + ci] = cc->ac ? (R)cc->ac[q] : R(0);
-        alph[s * nc + ci] = (R)cc->alph[q];
-        for (int t = 0; t < U * B; t++) {
-          coef[(s * U * B + t) * nc + ci] = (R)((t == (U - 1) * B && K.eshift[s] != 0.0)
-                                                    ? cc->coef[q * U * B + t] - K.eshift[s]
-                                                    : cc->coef[q * U * B + t]);
-          dco[(s * U * B + t) * nc + ci] = cc->dcoef ? (R)cc->dcoef[q * U * B + t] : R(0);
-        }
-        for (int u = 0; u < U; u++) lim[(s * U + u) * nc + ci] = cc->lim_u ? (R)cc->lim_u[q * U + u] : R(1);
-        ph[s * nc + ci] = (int8_t)cc->ph_state[q];
-        phb[s * nc + ci] = (int8_t)cc->ph_state_b[q];
-      }
-      for (int d = 0; d < D; d++) v[d * nc + ci] = (R)cc->v[3 * ci + d];
-      Pp[ci] = (R)cc->P[ci];
-      for (int t = 0; t < D * D; t++) gv[t * nc + ci] = cc->g_v ? (R)cc->g_v[ci * D * D + t] : R(0);
-      used[ci] = cc->used ? (int8_t)cc->used[ci] : 1;
+    if (!cc->rho || !cc->rhov || !cc->E || !cc->c || !cc->alph || !cc->coef || !cc->v || !cc->P || !cc->ph_state ||
+        !cc->ph_state_b) {
+      err = "upload_cells: a required array is NULL";
+      return PGDG_EINVAL;
     }
+    int rc = ensure_stage();
+    if (rc) return rc;
+    const int64_t nc = K.ncell;
+    int hk[XMAP_MAX];
+    double sh[XMAP_MAX];
+    /* per phase scalars: host [ci][s] */
+    const XferMap fs = xmap(F);
+    for (int s = 0; s < F; s++) sh[s] = K.eshift[s];
+    const XferMap fE = xmap(F, nullptr, sh);
+    /* momentum: host [ci][s][3] -> device [(s D + d)][ci] */
+    for (int s = 0; s < F; s++)
+      for (int d = 0; d < D; d++) hk[s * D + d] = s * 3 + d;
+    const XferMap fv = xmap(F * D, hk);
+    /* coefficients: host [ci][s][u][b] -> device [(s U + u) B + b][ci], energy constant shifted */
+    for (int t = 0; t < F * U * B; t++) sh[t] = (t % (U * B) == (U - 1) * B) ? K.eshift[t / (U * B)] : 0.0;
+    const XferMap fc = xmap(F * U * B, nullptr, sh);
+    const XferMap fd = xmap(F * U * B), fl = xmap(F * U), vec = xmap(D), gv = xmap(D * D), one = xmap(1);
     CK(cudaStreamSynchronize(st));
-    CK(cudaMemcpy(P.crho, rho.data(), sizeof(R) * rho.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.crhov, rhov.data(), sizeof(R) * rhov.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cE, E.data(), sizeof(R) * E.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cc, c.data(), sizeof(R) * c.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cac, ac.data(), sizeof(R) * ac.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.calph, alph.data(), sizeof(R) * alph.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.ccoef, coef.data(), sizeof(R) * coef.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cdcoef, dco.data(), sizeof(R) * dco.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.clim, lim.data(), sizeof(R) * lim.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cgv, gv.data(), sizeof(R) * gv.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cv, v.data(), sizeof(R) * v.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cP, Pp.data(), sizeof(R) * Pp.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cph, ph.data(), ph.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cphb, phb.data(), phb.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(P.cused, used.data(), used.size(), cudaMemcpyHostToDevice));
+    CK(xfer_h2d<R>(cc->rho, F, nc, fs, P.crho, nc, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(cc->rhov, 3 * F, nc, fv, P.crhov, nc, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(cc->E, F, nc, fE, P.cE, nc, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(cc->c, F, nc, fs, P.cc, nc, nullptr, nullptr, stage, st));
+    if (cc->ac) CK(xfer_h2d<R>(cc->ac, F, nc, fs, P.cac, nc, nullptr, nullptr, stage, st));
+    else CK(cudaMemsetAsync(P.cac, 0, sizeof(R) * F * nc, st));
+    CK(xfer_h2d<R>(cc->alph, F, nc, fs, P.calph, nc, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(cc->coef, F * U * B, nc, fc, P.ccoef, nc, nullptr, nullptr, stage, st));
+    if (cc->dcoef) CK(xfer_h2d<R>(cc->dcoef, F * U * B, nc, fd, P.cdcoef, nc, nullptr, nullptr, stage, st));
+    else CK(cudaMemsetAsync(P.cdcoef, 0, sizeof(R) * F * U * B * nc, st));
+    if (cc->lim_u) CK(xfer_h2d<R>(cc->lim_u, F * U, nc, fl, P.clim, nc, nullptr, nullptr, stage, st));
+    else fill_dev<R>(P.clim, (int64_t)F * U * nc, R(1), st);
+    if (cc->g_v) CK(xfer_h2d<R>(cc->g_v, D * D, nc, gv, P.cgv, nc, nullptr, nullptr, stage, st));
+    else CK(cudaMemsetAsync(P.cgv, 0, sizeof(R) * D * D * nc, st));
+    CK(xfer_h2d<R>(cc->v, 3, nc, vec, P.cv, nc, nullptr, nullptr, stage, st));
+    CK(xfer_h2d<R>(cc->P, 1, nc, one, P.cP, nc, nullptr, nullptr, stage, st));
+    CK(xfer_h2d_i8(cc->ph_state, F, nc, fs, P.cph, nc, stage, st));
+    CK(xfer_h2d_i8(cc->ph_state_b, F, nc, fs, P.cphb, nc, stage, st));
+    if (cc->used) CK(xfer_h2d_i8(cc->used, 1, nc, one, P.cused, nc, stage, st));
+    else CK(cudaMemsetAsync(P.cused, 1, (size_t)nc, st));
+    CK(cudaStreamSynchronize(st));
     return PGDG_OK;
   }
 
@@ -561,50 +556,36 @@ struct Ctx : pgdg_ctx {
       err = "cell count mismatch";
       return PGDG_EINVAL;
     }
+    int rc = ensure_stage();
+    if (rc) return rc;
     const int64_t nc = K.ncell;
-    std::vector<R> rho(F * nc), rhov(F * D * nc), E(F * nc), c(F * nc), ac(F * nc), alph(F * nc),
-        coef(F * U * B * nc), lim(F * U * nc), gv(D * D * nc), v(D * nc), Pp(nc), dco(F * U * B * nc);
-    std::vector<int8_t> ph(F * nc), phb(F * nc), used(nc);
+    int hk[XMAP_MAX];
+    double sh[XMAP_MAX];
+    const XferMap fs = xmap(F);
+    for (int s = 0; s < F; s++) sh[s] = K.eshift[s];
+    const XferMap fE = xmap(F, nullptr, sh);
+    for (int s = 0; s < F; s++)
+      for (int d = 0; d < D; d++) hk[s * D + d] = s * 3 + d;
+    const XferMap fv = xmap(F * D, hk);
+    for (int t = 0; t < F * U * B; t++) sh[t] = (t % (U * B) == (U - 1) * B) ? K.eshift[t / (U * B)] : 0.0;
+    const XferMap fc = xmap(F * U * B, nullptr, sh);
+    const XferMap fd = xmap(F * U * B), fl = xmap(F * U), vec = xmap(D), gv = xmap(D * D), one = xmap(1);
     CK(cudaStreamSynchronize(st));
-    CK(cudaMemcpy(rho.data(), P.crho, sizeof(R) * rho.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(rhov.data(), P.crhov, sizeof(R) * rhov.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(E.data(), P.cE, sizeof(R) * E.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(c.data(), P.cc, sizeof(R) * c.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(ac.data(), P.cac, sizeof(R) * ac.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(alph.data(), P.calph, sizeof(R) * alph.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(coef.data(), P.ccoef, sizeof(R) * coef.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(dco.data(), P.cdcoef, sizeof(R) * dco.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(lim.data(), P.clim, sizeof(R) * lim.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(gv.data(), P.cgv, sizeof(R) * gv.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(v.data(), P.cv, sizeof(R) * v.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(Pp.data(), P.cP, sizeof(R) * Pp.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(ph.data(), P.cph, ph.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(phb.data(), P.cphb, phb.size(), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(used.data(), P.cused, used.size(), cudaMemcpyDeviceToHost));
-    for (int64_t ci = 0; ci < nc; ci++) {
-      for (int s = 0; s < F; s++) {
-        int64_t q = ci * F + s;
-        if (co->rho) co->rho[q] = rho[s * nc + ci];
-        if (co->rhov) for (int d = 0; d < 3; d++) co->rhov[q * 3 + d] = d < D ? (double)rhov[(s * D + d) * nc + ci] : 0.0;
-        if (co->E) co->E[q] = K.eshift[s] != 0.0 ? (double)E[s * nc + ci] + K.eshift[s] : (double)E[s * nc + ci];
-        if (co->c) co->c[q] = c[s * nc + ci];
-        if (co->ac) co->ac[q] = ac[s * nc + ci];
-        if (co->alph) co->alph[q] = alph[s * nc + ci];
-        if (co->coef)
-          for (int t = 0; t < U * B; t++)
-            co->coef[q * U * B + t] = (t == (U - 1) * B && K.eshift[s] != 0.0)
-                                          ? (double)coef[(s * U * B + t) * nc + ci] + K.eshift[s]
-                                          : (double)coef[(s * U * B + t) * nc + ci];
-        if (co->dcoef) for (int t = 0; t < U * B; t++) co->dcoef[q * U * B + t] = dco[(s * U * B + t) * nc + ci];
-        if (co->lim_u) for (int u = 0; u < U; u++) co->lim_u[q * U + u] = lim[(s * U + u) * nc + ci];
-        if (co->ph_state) co->ph_state[q] = ph[s * nc + ci];
-        if (co->ph_state_b) co->ph_state_b[q] = phb[s * nc + ci];
-      }
-      if (co->v) for (int d = 0; d < 3; d++) co->v[3 * ci + d] = d < D ? (double)v[d * nc + ci] : 0.0;
-      if (co->P) co->P[ci] = Pp[ci];
-      if (co->used) co->used[ci] = used[ci];
-      if (co->g_v) for (int t = 0; t < D * D; t++) co->g_v[ci * D * D + t] = gv[t * nc + ci];
-    }
+    if (co->rho) CK(xfer_d2h<R>(P.crho, nc, nullptr, nc, fs, co->rho, F, nullptr, nullptr, stage, st));
+    if (co->rhov) CK(xfer_d2h<R>(P.crhov, nc, nullptr, nc, fv, co->rhov, 3 * F, nullptr, nullptr, stage, st));
+    if (co->E) CK(xfer_d2h<R>(P.cE, nc, nullptr, nc, fE, co->E, F, nullptr, nullptr, stage, st));
+    if (co->c) CK(xfer_d2h<R>(P.cc, nc, nullptr, nc, fs, co->c, F, nullptr, nullptr, stage, st));
+    if (co->ac) CK(xfer_d2h<R>(P.cac, nc, nullptr, nc, fs, co->ac, F, nullptr, nullptr, stage, st));
+    if (co->alph) CK(xfer_d2h<R>(P.calph, nc, nullptr, nc, fs, co->alph, F, nullptr, nullptr, stage, st));
+    if (co->coef) CK(xfer_d2h<R>(P.ccoef, nc, nullptr, nc, fc, co->coef, F * U * B, nullptr, nullptr, stage, st));
+    if (co->dcoef) CK(xfer_d2h<R>(P.cdcoef, nc, nullptr, nc, fd, co->dcoef, F * U * B, nullptr, nullptr, stage, st));
+    if (co->lim_u) CK(xfer_d2h<R>(P.clim, nc, nullptr, nc, fl, co->lim_u, F * U, nullptr, nullptr, stage, st));
+    if (co->g_v) CK(xfer_d2h<R>(P.cgv, nc, nullptr, nc, gv, co->g_v, D * D, nullptr, nullptr, stage, st));
+    if (co->v) CK(xfer_d2h<R>(P.cv, nc, nullptr, nc, vec, co->v, 3, nullptr, nullptr, stage, st));
+    if (co->P) CK(xfer_d2h<R>(P.cP, nc, nullptr, nc, one, co->P, 1, nullptr, nullptr, stage, st));
+    if (co->ph_state) CK(xfer_d2h_i8(P.cph, nc, nullptr, nc, fs, co->ph_state, F, stage, st));
+    if (co->ph_state_b) CK(xfer_d2h_i8(P.cphb, nc, nullptr, nc, fs, co->ph_state_b, F, stage, st));
+    if (co->used) CK(xfer_d2h_i8(P.cused, nc, nullptr, nc, one, co->used, 1, stage, st));
     return PGDG_OK;
   }
 

@@ -213,6 +213,38 @@ struct Launch {
   static int pst_variants();
 };
 
+/* ---------------- host <-> device layout conversion (k_xfer.cu) ---------------- */
+constexpr int XMAP_MAX = 48;
+/* device component k <- host component hk[k] (minus sh[k] on upload, plus on download) */
+struct XferMap {
+  int n;
+  int hk[XMAP_MAX];
+  double sh[XMAP_MAX];
+};
+XferMap xmap(int n, const int* hk = nullptr, const double* sh = nullptr);
+/* device staging buffer for raw host chunks */
+struct XferStage {
+  void* buf;
+  size_t bytes;
+};
+template <typename R>
+cudaError_t xfer_h2d(const double* host, int hstride, int64_t n, const XferMap& km, R* dev, int64_t dstride,
+                     const int8_t* grp, const double* gsh, XferStage& sg, cudaStream_t st);
+template <typename R>
+cudaError_t xfer_d2h(const R* dev, int64_t dstride, const int64_t* idx, int64_t n, const XferMap& km, double* host,
+                     int hstride, const int8_t* grp, const double* gsh, XferStage& sg, cudaStream_t st);
+cudaError_t xfer_h2d_i8(const int32_t* host, int hstride, int64_t n, const XferMap& km, int8_t* dev, int64_t dstride,
+                        XferStage& sg, cudaStream_t st);
+cudaError_t xfer_d2h_i8(const int8_t* dev, int64_t dstride, const int64_t* idx, int64_t n, const XferMap& km,
+                        int32_t* host, int hstride, XferStage& sg, cudaStream_t st);
+cudaError_t xfer_d2h_u64(const uint64_t* dev, const int64_t* idx, int64_t n, uint64_t* host, XferStage& sg,
+                         cudaStream_t st);
+void iota_u64(uint64_t* d, int64_t n, cudaStream_t st);
+template <typename R>
+void fill_dev(R* d, int64_t n, R v, cudaStream_t st);
+void alive_index(const int8_t* phase, unsigned long long* scan, unsigned long long* blk,
+                 const unsigned long long* d_n, int64_t cap, int64_t* idx, cudaStream_t st);
+
 /* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls, iterations, cap hits) */
 struct pgdg_mlp_fwd;
 int mgfm_seeded_run(void* net, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,

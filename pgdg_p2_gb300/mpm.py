@@ -151,18 +151,23 @@ class MPM:
         self._ck(lib().pgdg_num_particles(self.h, C.byref(n)), "num_particles")
         return n.value
 
-    def download_particles(self):
+    def download_particles(self, out=None):
+        """The live particles in canonical order (into `out` when given: a
+        Particles with room for them, e.g. in page-locked memory)."""
         n = self.num_particles()
-        p = Particles(n, self.dim)
+        p = out if out is not None else Particles(n, self.dim)
+        if p.cap < n:
+            raise PgdgError(-1, "download_particles: out too small")
         v = p.view()
         self._ck(lib().pgdg_download_particles(self.h, C.byref(v)), "download_particles")
+        p.n = int(v.n)
         return p
 
     def upload_cells(self, c: Cells):
         self._ck(lib().pgdg_upload_cells(self.h, C.byref(c.view())), "upload_cells")
 
-    def download_cells(self):
-        c = Cells(self.cs.ncells, self.dim)
+    def download_cells(self, out=None):
+        c = out if out is not None else Cells(self.cs.ncells, self.dim)
         self._ck(lib().pgdg_download_cells(self.h, C.byref(c.view())), "download_cells")
         return c
 

@@ -240,6 +240,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     g2.upload_particles(ph)
     g2.upload_cells(ch)
+    g2.set_iterate(0)              # the uploaded state is the initial one again
     for _ in range(ke):
         g2.advance(1)
         g2.stats()                 # device->host read of dt / max_v / counters

@@ -353,9 +353,12 @@ struct Ctx : pgdg_ctx {
     DevCounters h = counters();
     if (h.err) {
       char b[160];
-      snprintf(b, sizeof(b), "device status 0x%x (1 bucket, 2 list arena, 4 capacity, 8 missing list, 16 cell queue)",
+      snprintf(b, sizeof(b),
+               "device status 0x%x (1 bucket, 2 list arena, 4 capacity, 8 missing list, 16 cell queue, "
+               "64 no finite time step)",
                h.err);
       err = b;
+      if (h.err & ERR_DT) return PGDG_ENONFINITE;
       return (h.err & ERR_NOLIST) ? PGDG_ESTATE : PGDG_EOVERFLOW;
     }
     return PGDG_OK;

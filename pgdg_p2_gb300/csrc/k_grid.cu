@@ -199,6 +199,9 @@ template <typename R, bool EX>
 __global__ void k_dt_final(DevPtrs<R> P) {
   P.cnt->dt = __longlong_as_double((long long)P.cnt->dt_bits);
   P.cnt->max_v = __longlong_as_double((long long)P.cnt->maxv_bits);
+  /* no cell or particle gave a finite step (e.g. cells uploaded with zero
+   * sound speed while the iteration count selects the cell-based step) */
+  if (!(P.cnt->dt < 1.e19)) atomicOr(&P.cnt->err, ERR_DT);
 }
 
 template <int D, typename R, bool EX>

@@ -282,6 +282,12 @@ __device__ __forceinline__ double mgfm_f(double ul, double ur, double pl, double
   return ul - ur - (p - pl) / Wl - (p - pr) / Wr;
 }
 
+/* the seed from the baseline, the strength scale and the network output */
+__device__ __forceinline__ double seed_value(double pb, float sc, float y0, float my0, float sy0) {
+  const double ps = pb * (double)expf(sc * (y0 * sy0 + my0));
+  return ps > 1e-8 ? ps : 1e-8;
+}
+
 /* Seeds of a batch: features, network and seed p_b exp(sc y) in one pass per
  * problem; -1 (plain solve) for a problem without a positive root, f(1e-8) < 0,
  * evaluated with the clamps of the MGFM variant (mpm.cpp:886-893). */
@@ -319,8 +325,40 @@ __global__ void __launch_bounds__(128) k_seed(const float* __restrict__ params, 
 #pragma unroll
     for (int k = 0; k < NI; k++) xn[k] = (xn[k] - mx[k]) / sx[k];
     mlp_eval<1>(w, xn, y, nullptr, nullptr, nullptr, i);
-    double ps = pb * (double)expf(sc * (y[0] * sy0 + my0));
-    seed[i] = ps > 1e-8 ? ps : 1e-8;
+    seed[i] = seed_value(pb, sc, y[0], my0, sy0);
+  }
+}
+
+/* first half of the split seed path: features, baseline and strength scale
+ * of each problem (pb < 0 marks a problem without a positive root) */
+__global__ void k_seed_features(const double* __restrict__ in6, const int8_t* __restrict__ mat2,
+                                const double* __restrict__ gam, const double* __restrict__ pinf, int variant,
+                                float* __restrict__ X, double* __restrict__ pb_out, float* __restrict__ sc_out,
+                                int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double* q = in6 + 6 * i;
+    const int s = mat2[2 * i], s1 = mat2[2 * i + 1];
+    const double gl = gam[s], il = pinf[s], gr = gam[s1], ir = pinf[s1];
+    double pl = q[2], pr = q[3], rl = q[4], rr = q[5];
+    if (variant == 0) {
+      pl = amax1(pl, 1e-10);
+      pr = amax1(pr, 1e-10);
+      rl = amax1(rl, 1e-10);
+      rr = amax1(rr, 1e-10);
+    } else {
+      if (pl < 0) pl = 0;
+      if (pr < 0) pr = 0;
+    }
+    if (mgfm_f(q[0], q[1], pl, pr, rl, rr, gl, il, gr, ir, 1e-8) < 0) {
+      pb_out[i] = -1.0;
+      continue;
+    }
+    double pb;
+    float sc, x[NI];
+    mgfm_features(q, gl, il, gr, ir, x, &pb, &sc);
+    for (int k = 0; k < NI; k++) X[i * NI + k] = x[k];
+    pb_out[i] = pb;
+    sc_out[i] = sc;
   }
 }
 
@@ -330,14 +368,19 @@ __global__ void __launch_bounds__(128) k_seed(const float* __restrict__ params, 
 __global__ void k_mgfm_seeded(const double* __restrict__ in6, const int8_t* __restrict__ mat2,
                               const double* __restrict__ gam, const double* __restrict__ pinf, int variant,
                               const double* __restrict__ seed, double* __restrict__ out3, int32_t* __restrict__ iters,
-                              int64_t n, unsigned long long* stats) {
+                              int64_t n, unsigned long long* stats, const float* __restrict__ Y,
+                              const float* __restrict__ sc, const float* __restrict__ params) {
   unsigned long long nit = 0, nmax = 0, ncall = 0;
+  const float my0 = params ? params[NPARAM + 2 * NI] : 0.f, sy0 = params ? params[NPARAM + 2 * NI + NO] : 1.f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double* q = in6 + 6 * i;
     int s = mat2[2 * i], s1 = mat2[2 * i + 1];
     double o[3];
     int it = 0;
-    const double sd = seed ? seed[i] : -1.0;
+    /* seed: given, or (split path) formed from the baseline in seed[], the
+     * scale and the network output */
+    double sd = seed ? seed[i] : -1.0;
+    if (Y && sd > 0) sd = seed_value(sd, sc[i], Y[i * NO], my0, sy0);
     bool done = false;
     if (sd > 0) {
       it = mgfm(q[0], q[1], q[2], q[3], q[4], q[5], gam[s], pinf[s], gam[s1], pinf[s1], variant, sd, o);
@@ -376,14 +419,18 @@ struct pgdg_mlp {
         *dZ3 = nullptr, *dZ2 = nullptr, *dZ1 = nullptr;
   double* d_loss = nullptr;
   int64_t cap = 0;
-  double* seeds = nullptr; /* per-problem seeds of batched solves */
+  double* seeds = nullptr; /* per-problem seeds (or baselines) of batched solves */
+  float* sc = nullptr;     /* per-problem strength scale of the split seed path */
   int64_t seeds_cap = 0;
   int reserve_seeds(int64_t n) {
     if (n <= seeds_cap) return PGDG_OK;
     if (seeds) cudaFree(seeds);
+    if (sc) cudaFree(sc);
     seeds = nullptr;
+    sc = nullptr;
     seeds_cap = 0;
     if (cudaMalloc((void**)&seeds, sizeof(double) * n) != cudaSuccess) return PGDG_ENOMEM;
+    if (cudaMalloc((void**)&sc, sizeof(float) * n) != cudaSuccess) return PGDG_ENOMEM;
     seeds_cap = n;
     return PGDG_OK;
   }
@@ -404,6 +451,7 @@ struct pgdg_mlp {
       if (b) cudaFree(b);
     if (d_loss) cudaFree(d_loss);
     if (seeds) cudaFree(seeds);
+    if (sc) cudaFree(sc);
   }
 };
 
@@ -563,7 +611,8 @@ int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8
     seed_launch(const_cast<pgdg_mlp*>(net), in6, mat2, gam, pinf, variant, seeds, n, 0);
     sd = seeds;
   }
-  k_mgfm_seeded<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, nullptr);
+  k_mgfm_seeded<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, nullptr, nullptr, nullptr,
+                                        nullptr);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 
@@ -575,14 +624,21 @@ int mgfm_seeded_run(void* netv, const double* in6, const int8_t* mat2, const dou
                     cudaStream_t st) {
   if (n <= 0) return PGDG_OK;
   pgdg_mlp* m = static_cast<pgdg_mlp*>(netv);
-  const double* sd = nullptr;
-  if (m) {
-    int rc = m->reserve_seeds(n);
-    if (rc) return rc;
-    seed_launch(m, in6, mat2, gam, pinf, variant, m->seeds, n, st);
-    sd = m->seeds;
+  if (!m) {
+    k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, nullptr, out3, iters, n, stats,
+                                                 nullptr, nullptr, nullptr);
+    return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
   }
-  k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, stats);
+  /* split seed path: features and baseline, the network, then Newton with the
+   * seed formed per problem (same arithmetic as the fused k_seed) */
+  int rc = m->reserve_seeds(n);
+  if (rc) return rc;
+  rc = m->reserve(n);
+  if (rc) return rc;
+  k_seed_features<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, m->X, m->seeds, m->sc, n);
+  forward(m, m->X, m->Y, nullptr, nullptr, nullptr, n, st);
+  k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, m->seeds, out3, iters, n, stats, m->Y,
+                                               m->sc, m->d_params);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 }  // namespace pgdg

@@ -35,6 +35,7 @@ enum : uint32_t {
   ERR_NOLIST = 1u << 3,    /* split/merge needed a list the device did not keep */
   ERR_CELLQ = 1u << 4,     /* flagged-cell queue overflowed */
   ERR_QUEUE = 1u << 5,     /* interface queue overflowed */
+  ERR_DT = 1u << 6,        /* no finite CFL time step */
 };
 
 struct DevCounters {

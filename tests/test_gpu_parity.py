@@ -91,3 +91,35 @@ def test_fp64_methods_bitwise_c3(gpu_mod, oracle_mod):
             g.Update_particle(md)
             o.Update_particle(md)
             assert particles_bitwise_equal(g.download_particles(), o.download_particles()) == [], "G2P/shift"
+
+
+def test_reupload_restarts_exactly(gpu_mod):
+    """Uploading a state into a context that has run steps, with the iteration
+    count restarted, continues bit for bit like a fresh context; without the
+    restart the cell-based CFL step of the (zero sound-speed) initial cells is
+    reported as PGDG_ENONFINITE instead of being used."""
+    from pgdg_p2_gb300.abi import PREC_FP64, PgdgError
+    M = gpu_mod
+    cs, p, c = M.make_case(3, (48, 12, 12))
+    fresh = M.MPM(cs, PREC_FP64)
+    fresh.upload_particles(p)
+    fresh.upload_cells(c)
+    fresh.advance(2)
+    g = M.MPM(cs, PREC_FP64)
+    g.upload_particles(p)
+    g.upload_cells(c)
+    g.advance(3)
+    g.upload_particles(p)
+    g.upload_cells(c)
+    g.set_iterate(0)
+    g.advance(2)
+    g.sync()
+    assert particles_bitwise_equal(g.download_particles(), fresh.download_particles()) == []
+    assert cells_bitwise_equal(g.download_cells(), fresh.download_cells()) == []
+    g.upload_particles(p)
+    g.upload_cells(c)
+    g.set_iterate(5)
+    g.advance(1)
+    with pytest.raises(PgdgError) as ei:
+        g.sync()
+    assert ei.value.code == -4   # PGDG_ENONFINITE

@@ -142,6 +142,7 @@ struct Ctx : pgdg_ctx {
   int x0b = 0;          /* step-start coordinate buffer (md 1) */
   double* d_tot = nullptr;
   IfaceQ Q{};
+  PartScratch part;   /* root partition of the interface batch */
   double *d_gam = nullptr, *d_pinf = nullptr;
   unsigned long long* d_ncell = nullptr;
 
@@ -156,6 +157,7 @@ struct Ctx : pgdg_ctx {
     if (st) cudaStreamSynchronize(st);
     for (auto e : ev_pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
+    part.release();
     if (st) cudaStreamDestroy(st);
   }
 
@@ -845,7 +847,8 @@ struct Ctx : pgdg_ctx {
     iface_last = n;
     int rc = PGDG_OK;
     timed("mgfm_seeded", 3, [&] {
-      rc = mgfm_seeded_run(net, Q.in6, Q.mat, d_gam, d_pinf, K.mgfm_variant, Q.out3, nullptr, n, &P.cnt->mgfm_calls, st);
+      rc = mgfm_seeded_run(net, Q.in6, Q.mat, d_gam, d_pinf, K.mgfm_variant, Q.out3, nullptr, n, &P.cnt->mgfm_calls,
+                           part, st);
     });
     if (rc) return rc;
     timed("grid_acc", 1, [&] { Launch<D, R, EX>::grid_acc_queued(K, P, Q, st); });

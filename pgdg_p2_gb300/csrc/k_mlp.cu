@@ -362,6 +362,48 @@ __global__ void k_seed_features(const double* __restrict__ in6, const int8_t* __
   }
 }
 
+/* partition of a batch by the existence of a positive root: a problem without
+ * one runs the plain Newton solve down to the 1e-8 floor (about 30 iterations)
+ * while a seeded one converges in two or three, so the two kinds are solved in
+ * separate warps.  flag[i] = 1 for a problem with a root (pb > 0 when the seed
+ * path computed it, else f(1e-8) >= 0 evaluated here). */
+__global__ void k_root_flag(const double* __restrict__ in6, const int8_t* __restrict__ mat2,
+                            const double* __restrict__ gam, const double* __restrict__ pinf, int variant,
+                            const double* __restrict__ pb, unsigned long long* __restrict__ flag, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    bool root;
+    if (pb) {
+      root = pb[i] > 0;
+    } else {
+      const double* q = in6 + 6 * i;
+      const int s = mat2[2 * i], s1 = mat2[2 * i + 1];
+      double pl = q[2], pr = q[3], rl = q[4], rr = q[5];
+      if (variant == 0) {
+        pl = amax1(pl, 1e-10);
+        pr = amax1(pr, 1e-10);
+        rl = amax1(rl, 1e-10);
+        rr = amax1(rr, 1e-10);
+      } else {
+        if (pl < 0) pl = 0;
+        if (pr < 0) pr = 0;
+      }
+      root = !(mgfm_f(q[0], q[1], pl, pr, rl, rr, gam[s], pinf[s], gam[s1], pinf[s1], 1e-8) < 0);
+    }
+    flag[i] = root ? 1ull : 0ull;
+  }
+}
+/* order: problems with a root first, then the others, each in input order;
+ * pos is the exclusive prefix of the flags, nroot_p their total */
+__global__ void k_root_perm(const unsigned long long* __restrict__ pos, const unsigned long long* __restrict__ nroot_p,
+                            int32_t* __restrict__ perm, int64_t n) {
+  const int64_t nroot = (int64_t)*nroot_p;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = (int64_t)pos[i];
+    const bool root = (i + 1 < n ? (int64_t)pos[i + 1] : nroot) > p;
+    perm[root ? p : nroot + (i - p)] = (int32_t)i;
+  }
+}
+
 /* Newton from the seed (or the plain seed when seed is NULL or the entry is
  * negative); a seeded solve that has not converged at the cap is redone from
  * the plain seed, and its iterations are counted together */
@@ -369,10 +411,12 @@ __global__ void k_mgfm_seeded(const double* __restrict__ in6, const int8_t* __re
                               const double* __restrict__ gam, const double* __restrict__ pinf, int variant,
                               const double* __restrict__ seed, double* __restrict__ out3, int32_t* __restrict__ iters,
                               int64_t n, unsigned long long* stats, const float* __restrict__ Y,
-                              const float* __restrict__ sc, const float* __restrict__ params) {
+                              const float* __restrict__ sc, const float* __restrict__ params,
+                              const int32_t* __restrict__ perm) {
   unsigned long long nit = 0, nmax = 0, ncall = 0;
   const float my0 = params ? params[NPARAM + 2 * NI] : 0.f, sy0 = params ? params[NPARAM + 2 * NI + NO] : 1.f;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm ? (int64_t)perm[j] : j;
     const double* q = in6 + 6 * i;
     int s = mat2[2 * i], s1 = mat2[2 * i + 1];
     double o[3];
@@ -419,6 +463,7 @@ struct pgdg_mlp {
         *dZ3 = nullptr, *dZ2 = nullptr, *dZ1 = nullptr;
   double* d_loss = nullptr;
   int64_t cap = 0;
+  PartScratch part;         /* root partition of batched solves */
   double* seeds = nullptr; /* per-problem seeds (or baselines) of batched solves */
   float* sc = nullptr;     /* per-problem strength scale of the split seed path */
   int64_t seeds_cap = 0;
@@ -452,6 +497,7 @@ struct pgdg_mlp {
     if (d_loss) cudaFree(d_loss);
     if (seeds) cudaFree(seeds);
     if (sc) cudaFree(sc);
+    part.release();
   }
 };
 
@@ -578,7 +624,16 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
                       const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n) {
   if (n < 0 || !in6 || !mat2 || !gam || !pinf || !out3 || nmat < 1) return PGDG_EINVAL;
   if (n == 0) return PGDG_OK;
-  return mgfm_seeded_run((void*)net, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr, 0);
+  /* partition scratch: the network's, or (plain seed) a per-device cache used
+   * under a lock; calls run on the default stream */
+  if (net) return mgfm_seeded_run((void*)net, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr,
+                                  const_cast<pgdg_mlp*>(net)->part, 0);
+  static PartScratch cache[64];
+  static std::mutex mu;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PGDG_ECUDA;
+  std::lock_guard<std::mutex> lk(mu);
+  return mgfm_seeded_run(nullptr, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr, cache[dev], 0);
 }
 
 /* Seeds of pgdg_mgfm_batched_noalloc: a file-scope device array, so the call
@@ -612,33 +667,71 @@ int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8
     sd = seeds;
   }
   k_mgfm_seeded<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, nullptr, nullptr, nullptr,
-                                        nullptr);
+                                        nullptr, nullptr);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 
 }  // extern "C"
 
 namespace pgdg {
+int PartScratch::reserve(int64_t n) {
+  if (n <= cap) return PGDG_OK;
+  if (pos) cudaFree(pos);
+  if (blk) cudaFree(blk);
+  if (perm) cudaFree(perm);
+  if (dn) cudaFree(dn);
+  pos = blk = dn = nullptr;
+  perm = nullptr;
+  cap = 0;
+  if (cudaMalloc((void**)&pos, sizeof(unsigned long long) * (size_t)(n + 1)) != cudaSuccess ||
+      cudaMalloc((void**)&blk, sizeof(unsigned long long) * (size_t)(n / 2048 + 2)) != cudaSuccess ||
+      cudaMalloc((void**)&perm, sizeof(int32_t) * (size_t)n) != cudaSuccess ||
+      cudaMalloc((void**)&dn, sizeof(unsigned long long)) != cudaSuccess)
+    return PGDG_ENOMEM;
+  cap = n;
+  return PGDG_OK;
+}
+void PartScratch::release() {
+  if (pos) cudaFree(pos);
+  if (blk) cudaFree(blk);
+  if (perm) cudaFree(perm);
+  if (dn) cudaFree(dn);
+  pos = blk = dn = nullptr;
+  perm = nullptr;
+  cap = 0;
+}
+
 int mgfm_seeded_run(void* netv, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
                     int variant, double* out3, int32_t* iters, int64_t n, unsigned long long* stats,
-                    cudaStream_t st) {
+                    PartScratch& ps, cudaStream_t st) {
   if (n <= 0) return PGDG_OK;
+  if (n > INT32_MAX) return PGDG_EINVAL;
   pgdg_mlp* m = static_cast<pgdg_mlp*>(netv);
-  if (!m) {
-    k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, nullptr, out3, iters, n, stats,
-                                                 nullptr, nullptr, nullptr);
-    return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
+  int rc = ps.reserve(n);
+  if (rc) return rc;
+  const double* sd = nullptr;
+  if (m) {
+    /* split seed path: features and baseline, the network, then Newton with the
+     * seed formed per problem (same arithmetic as the fused k_seed) */
+    rc = m->reserve_seeds(n);
+    if (rc) return rc;
+    rc = m->reserve(n);
+    if (rc) return rc;
+    k_seed_features<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, m->X, m->seeds, m->sc, n);
+    forward(m, m->X, m->Y, nullptr, nullptr, nullptr, n, st);
+    sd = m->seeds;
   }
-  /* split seed path: features and baseline, the network, then Newton with the
-   * seed formed per problem (same arithmetic as the fused k_seed) */
-  int rc = m->reserve_seeds(n);
-  if (rc) return rc;
-  rc = m->reserve(n);
-  if (rc) return rc;
-  k_seed_features<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, m->X, m->seeds, m->sc, n);
-  forward(m, m->X, m->Y, nullptr, nullptr, nullptr, n, st);
-  k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, m->seeds, out3, iters, n, stats, m->Y,
-                                               m->sc, m->d_params);
+  /* problems with a root first: warps of converging problems are not held up
+   * by the long floor descent of problems without one (results per problem
+   * are unchanged) */
+  const unsigned long long nn = (unsigned long long)n;
+  cudaMemcpyAsync(ps.dn, &nn, sizeof(nn), cudaMemcpyHostToDevice, st);
+  k_root_flag<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, ps.pos, n);
+  scan_u64(ps.pos, ps.blk, ps.dn, n, st);
+  k_root_perm<<<g_for(n, 256), 256, 0, st>>>(ps.pos, ps.blk + (n + 2047) / 2048, ps.perm, n);
+  k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, stats,
+                                               m ? m->Y : nullptr, m ? m->sc : nullptr, m ? m->d_params : nullptr,
+                                               ps.perm);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 }  // namespace pgdg

@@ -247,10 +247,17 @@ void alive_index(const int8_t* phase, unsigned long long* scan, unsigned long lo
                  const unsigned long long* d_n, int64_t cap, int64_t* idx, cudaStream_t st);
 
 /* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls, iterations, cap hits) */
-struct pgdg_mlp_fwd;
+/* scratch of the root partition of a batch (prefix, block sums, order, count) */
+struct PartScratch {
+  unsigned long long *pos = nullptr, *blk = nullptr, *dn = nullptr;
+  int32_t* perm = nullptr;
+  int64_t cap = 0;
+  int reserve(int64_t n);
+  void release();
+};
 int mgfm_seeded_run(void* net, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
                     int variant, double* out3, int32_t* iters, int64_t n, unsigned long long* stats,
-                    cudaStream_t st);
+                    PartScratch& ps, cudaStream_t st);
 
 /* shared helpers used by several translation units */
 int grid_for(int64_t n, int block);

@@ -28,10 +28,16 @@ sys.path.insert(0, HERE)
 
 METRIC = "cell-stage updates/s, learned+mixed vs plain FP64 on GB300 at matched L1 error"
 UNIT = "cell-stage/s"
-WORKLOAD = "3D Air/He spherical shock-bubble, 384x96x96 P1 DG cells, 8 particles/cell"
+# workloads: config id -> (description, grid, bounded CPU sample grid); the
+# default (and the metric's) is the spherical shock-bubble
+WORKLOADS = {
+    1: ("2D two-phase triple point, 112x48 P1 DG cells, 4 particles/cell", (112, 48, 1), (112, 48, 1)),
+    2: ("3D Air/He cylindrical shock-bubble, 256x64x64 P1 DG cells, 8 particles/cell", (256, 64, 64), (64, 16, 16)),
+    3: ("3D Air/He spherical shock-bubble, 384x96x96 P1 DG cells, 8 particles/cell", (384, 96, 96), (96, 24, 24)),
+    4: ("2D underwater explosion, 1024x1024 P1 DG cells, 4 particles/cell", (1024, 1024, 1), (256, 256, 1)),
+}
 CONFIG_ID = 3
-GRID = (384, 96, 96)
-SAMPLE_GRID = (96, 24, 24)      # bounded CPU sample of the same case
+WORKLOAD, GRID, SAMPLE_GRID = WORKLOADS[CONFIG_ID]
 
 
 def _dist():
@@ -39,6 +45,21 @@ def _dist():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def replica_value(ms, cells_per_rank, steps):
+    """Whole-job cell-stage/s of N independent replicas (one per GPU, no
+    exchange between them): all ranks' cell-stages over the slowest rank's time.
+    Returns (max ms over ranks, value)."""
+    ws, _, _ = _dist()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, ws * cells_per_rank * 2 * steps / (ms / 1e3)
 
 
 class Clocks:
@@ -200,14 +221,8 @@ def run_ours(args):
     g.profile(False)
     launches = g.launch_count() - n0
     barrier()
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = replica_value(ms, ncell, args.steps)
     st = g.stats()
-    value = ws * ncell * 2 * args.steps / (ms / 1e3)
 
     if args.only_timed:
         if rank == 0:
@@ -407,7 +422,12 @@ def main():
     ap.add_argument("--no-c5", action="store_true", help="skip the batched MGFM micro-benchmark")
     ap.add_argument("--only-timed", action="store_true", help="timed region only (profiling runs)")
     ap.add_argument("--grid", default="", help="override the grid, e.g. 192,48,48 (profiling runs)")
+    ap.add_argument("--config", type=int, default=3, choices=sorted(WORKLOADS),
+                    help="workload: 1 triple point, 2 cylinder, 3 sphere (default, the metric's), 4 underwater explosion")
     args = ap.parse_args()
+    global CONFIG_ID, WORKLOAD, GRID, SAMPLE_GRID
+    CONFIG_ID = args.config
+    WORKLOAD, GRID, SAMPLE_GRID = WORKLOADS[CONFIG_ID]
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -194,7 +194,7 @@ def run_ours(args):
     params = S.load_default()
     if params is None:
         raise SystemExit("trained seed weights missing (python -m pgdg_p2_gb300.train_surrogate)")
-    net = S.Surrogate(params)
+    net = S.Surrogate(params, tc=True)
 
     grid = tuple(int(x) for x in args.grid.split(",")) if args.grid else GRID
     cs, p, c = M.make_case(CONFIG_ID, grid)
@@ -350,7 +350,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "cells": ncell, "particles": st["n_particles"],
                            "precision": "mixed: FP32 DG residual/limiter/G2P/shifting, FP64 MGFM Newton and P2G "
-                                        "moment sums", "mgfm_seed": "learned (12-64-64-64-2 MLP, BF16 weights) with plain-Newton fallback; interface problems batched per stage",
+                                        "moment sums", "mgfm_seed": "learned (12-64-64-64-2 MLP, BF16 weights and activations on tcgen05 tensor cores) with plain-Newton fallback; interface problems batched per stage",
                            "l2": "inputs larger than L2 (state of several GB streamed every step)",
                            "parallelism": f"replicas x{ws}"},
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,

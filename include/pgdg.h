@@ -89,8 +89,10 @@ int pgdg_totals(pgdg_ctx* ctx, double* out6);                      /* conservati
 /* ---- MGFM seed surrogate (new; the reference starts Newton from max(p_l,p_r),
  *      mpm.cpp:893) ----
  * A 12-64-64-64-2 tanh MLP predicting the star pressure and velocity of a
- * two-material Riemann problem; BF16 weights (bf16 = 1) or FP32 weights
- * (bf16 = 0, for gradient checks), FP32 accumulation.  Parameters are
+ * two-material Riemann problem, FP32 accumulation.  bf16 = 1: BF16 weights,
+ * FP32 activations (CUDA cores); 0: FP32 weights (gradient checks); 2: BF16
+ * weights and activations on the tensor cores (tcgen05) for forward passes,
+ * training as mode 1.  Parameters are
  * pgdg_surrogate_num_params() floats: weights, biases and the fixed
  * feature/target normalisation.  Array arguments are device pointers unless
  * named *_host. */
@@ -140,7 +142,9 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
  * written, so nothing is cleared.  The first call on a device looks the array
  * up (cudaGetSymbolAddress) and should come before any stream capture.
  * Overlapping calls on one device (several host threads, or per-thread default
- * streams) share the array and race: serialise them.  Device pointers; the
+ * streams) share the array and race: serialise them.  A tensor-core network
+ * (pgdg_surrogate_create mode 2) is refused (PGDG_EINVAL): its seeds differ from
+ * the CUDA-core network this entry point evaluates.  Device pointers; the
  * default stream. */
 #define PGDG_MGFM_NOALLOC_MAX (1 << 20)
 int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8_t* mat2, const double* gam,

@@ -455,6 +455,8 @@ using namespace pgdg;
 
 struct pgdg_mlp {
   int bf16 = 1;
+  int tc = 0;           /* forward passes on the tensor cores (BF16 activations) */
+  int* d_tcerr = nullptr;
   float* d_params = nullptr; /* NPARAM + NNORM */
   float *d_m = nullptr, *d_v = nullptr, *d_g = nullptr;
   int64_t step = 0;
@@ -497,6 +499,7 @@ struct pgdg_mlp {
     if (d_loss) cudaFree(d_loss);
     if (seeds) cudaFree(seeds);
     if (sc) cudaFree(sc);
+    if (d_tcerr) cudaFree(d_tcerr);
     part.release();
   }
 };
@@ -508,6 +511,10 @@ inline int g_for(int64_t n, int b) {
   return g < 1 ? 1 : (int)g;
 }
 void forward(pgdg_mlp* m, const float* X, float* Y, float* A1, float* A2, float* A3, int64_t n, cudaStream_t st) {
+  if (m->tc && !A1) {
+    mlp_tc_forward(m->d_params, X, Y, n, m->d_tcerr, st);
+    return;
+  }
   if (m->bf16) k_mlp_forward<true><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n);
   else k_mlp_forward<false><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n);
 }
@@ -543,8 +550,15 @@ extern "C" {
 int pgdg_surrogate_create(int bf16, pgdg_mlp** out) {
   int dev = 0;
   if (cudaGetDeviceCount(&dev) != cudaSuccess || dev < 1) return PGDG_ECUDA;
+  if (bf16 < 0 || bf16 > 2) return PGDG_EINVAL;
   pgdg_mlp* m = new pgdg_mlp();
   m->bf16 = bf16 ? 1 : 0;
+  m->tc = bf16 == 2 ? 1 : 0;
+  if (cudaMalloc((void**)&m->d_tcerr, sizeof(int)) != cudaSuccess) {
+    delete m;
+    return PGDG_ENOMEM;
+  }
+  cudaMemset(m->d_tcerr, 0, sizeof(int));
   const size_t np = NPARAM + NNORM;
   if (cudaMalloc((void**)&m->d_params, sizeof(float) * np) != cudaSuccess ||
       cudaMalloc((void**)&m->d_m, sizeof(float) * NPARAM) != cudaSuccess ||
@@ -585,7 +599,13 @@ int pgdg_surrogate_features(const double* in6, const int8_t* mat2, const double*
 int pgdg_surrogate_forward(pgdg_mlp* m, const float* X, float* Y, int64_t n) {
   if (n <= 0) return PGDG_OK;
   forward(m, X, Y, nullptr, nullptr, nullptr, n, 0);
-  return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
+  if (cudaGetLastError() != cudaSuccess) return PGDG_ECUDA;
+  if (m->tc) {
+    int e = 0;
+    if (cudaMemcpy(&e, m->d_tcerr, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return PGDG_ECUDA;
+    if (e) return PGDG_ETIMEOUT;
+  }
+  return PGDG_OK;
 }
 /* gradient of the loss 1/(2n) sum |Y - normalise(T)|^2 ... returned to the host
  * (NPARAM floats) together with the loss */
@@ -645,6 +665,7 @@ int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8
                               const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n) {
   if (n < 0 || !in6 || !mat2 || !gam || !pinf || !out3 || nmat < 1) return PGDG_EINVAL;
   if (n > PGDG_MGFM_NOALLOC_MAX) return PGDG_EOVERFLOW;
+  if (net && net->tc) return PGDG_EINVAL; /* its seeds come from the SIMT network only */
   if (n == 0) return PGDG_OK;
   const double* sd = nullptr;
   if (net) {

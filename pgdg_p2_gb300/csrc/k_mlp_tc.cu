@@ -1,0 +1,259 @@
+/*
+ * k_mlp_tc.cu -- forward pass of the MGFM seed surrogate on the tensor cores
+ * (tcgen05): the 12-64-64-64-2 tanh network over tiles of 128 problems.
+ *
+ * One CTA of 128 threads holds the BF16 weights in shared memory in the
+ * canonical K-major layout without swizzle (8 x 8 core matrices of 128 bytes;
+ * element (r, k) of an R x K operand at ((r/8)(K/8) + k/8) * 128 + (r%8) * 16 +
+ * (k%8) * 2, so LBO = 128 B between core matrices along K and SBO = (K/8) * 128 B
+ * between 8-row groups).  Per tile and layer:
+ *   - each thread writes its problem's row of the A operand (BF16: the
+ *     normalised features, then the previous layer's tanh activations),
+ *   - one thread issues tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 -> FP32,
+ *     M = 128, N = 64, or 16 for the padded output layer, K in steps of 16)
+ *     into tensor memory and commits to an mbarrier,
+ *   - every thread waits (bounded), reads its row of the accumulator with
+ *     tcgen05.ld.32x32b, adds the bias and applies tanh.
+ * Layer 1's K of 12 is padded to 16 and the output layer's N of 2 to 16 with
+ * zero weights.  Against the SIMT forward (FP32 activations, tanhf) the
+ * activations here are BF16 (tanh in hardware precision), so outputs differ at
+ * the 1e-2 level; the seeded Newton solve judges the seed either way.
+ *
+ * Waits give up after a fixed number of polls: the kernel then records an
+ * error, stops issuing work, frees its tensor memory and returns.
+ */
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "pgdg_dev.cuh"
+
+namespace pgdg {
+
+namespace {
+constexpr int NI_ = 12, NH_ = 64, NO_ = 2;
+constexpr int OW1 = 0, OB1 = OW1 + NH_ * NI_, OW2 = OB1 + NH_, OB2 = OW2 + NH_ * NH_, OW3 = OB2 + NH_,
+              OB3 = OW3 + NH_ * NH_, OW4 = OB3 + NH_, OB4 = OW4 + NO_ * NH_, NPAR_ = OB4 + NO_;
+constexpr int K1 = 16;    /* layer-1 K: 12 features padded */
+constexpr int N4 = 16;    /* output layer N: 2 outputs padded */
+constexpr int TILE = 128; /* problems per tile = M */
+/* tensor memory columns held per CTA (the accumulator is 128 lanes x 64
+ * columns); several CTAs share an SM's 512 columns */
+constexpr uint32_t TMEM_COLS = 64;
+
+/* shared memory layout (bytes; every operand starts on a 1024-byte boundary) */
+constexpr int S_W1 = 0;                        /* 64 x 16 */
+constexpr int S_W2 = S_W1 + NH_ * K1 * 2;      /* 64 x 64 */
+constexpr int S_W3 = S_W2 + NH_ * NH_ * 2;     /* 64 x 64 */
+constexpr int S_W4 = S_W3 + NH_ * NH_ * 2;     /* 16 x 64 */
+constexpr int S_A0 = S_W4 + N4 * NH_ * 2;      /* 128 x 16 */
+constexpr int S_A = S_A0 + TILE * K1 * 2;      /* 128 x 64 */
+constexpr int S_F = S_A + TILE * NH_ * 2;      /* floats: b1 b2 b3 (64 each), b4 (16), mx sx (12 each) */
+constexpr int F_B1 = 0, F_B2 = 64, F_B3 = 128, F_B4 = 192, F_MX = 208, F_SX = 220, F_N = 232;
+constexpr int S_MBAR = S_F + 1024;
+constexpr int S_TSLOT = S_MBAR + 16;
+constexpr int S_TOTAL = S_TSLOT + 16;
+static_assert(S_W2 % 1024 == 0 && S_W3 % 1024 == 0 && S_W4 % 1024 == 0 && S_A0 % 1024 == 0 && S_A % 1024 == 0,
+              "operand alignment");
+static_assert(F_N * 4 <= 1024, "float block");
+
+__device__ __forceinline__ int kmaj(int r, int k, int K) {
+  return ((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+/* shared-memory matrix descriptor: no swizzle, K-major */
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46; /* descriptor version of this architecture */
+  return d;
+}
+
+/* instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major */
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t cnt) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(cnt) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+/* bounded wait for a phase of the mbarrier */
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); it++)
+    if (mbar_try(a, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+/* 16 consecutive accumulator columns of this thread's row */
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+/* hardware tanh (relative error about 2^-11, below the BF16 rounding of the
+ * activation that follows) */
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+/* accumulator row -> bias + tanh -> BF16 row of the next A operand */
+__device__ __forceinline__ void hidden_epilogue(uint32_t trow, const float* bias, unsigned char* sA, int row) {
+  for (int c = 0; c < NH_; c += 16) {
+    uint32_t r[16];
+    tmem_ld16(trow + (uint32_t)c, r);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const float h = tanh_hw(__uint_as_float(r[j]) + bias[c + j]);
+      *reinterpret_cast<__nv_bfloat16*>(sA + kmaj(row, c + j, NH_)) = __float2bfloat16_rn(h);
+    }
+  }
+}
+}  // namespace
+
+__global__ void __launch_bounds__(128, 4) k_mlp_tc(const float* __restrict__ params, const float* __restrict__ X,
+                                                   float* __restrict__ Y, int64_t n, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int t = threadIdx.x, warp = t >> 5;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+  float* fb = reinterpret_cast<float*>(sm + S_F);
+
+  /* weights in the canonical layout (BF16, padded), biases and normalisation */
+  for (int e = t; e < NH_ * K1; e += blockDim.x) {
+    const int r = e / K1, k = e % K1;
+    const float v = k < NI_ ? params[OW1 + r * NI_ + k] : 0.f;
+    *reinterpret_cast<__nv_bfloat16*>(sm + S_W1 + kmaj(r, k, K1)) = __float2bfloat16_rn(v);
+  }
+  for (int e = t; e < NH_ * NH_; e += blockDim.x) {
+    const int r = e / NH_, k = e % NH_;
+    *reinterpret_cast<__nv_bfloat16*>(sm + S_W2 + kmaj(r, k, NH_)) = __float2bfloat16_rn(params[OW2 + e]);
+    *reinterpret_cast<__nv_bfloat16*>(sm + S_W3 + kmaj(r, k, NH_)) = __float2bfloat16_rn(params[OW3 + e]);
+  }
+  for (int e = t; e < N4 * NH_; e += blockDim.x) {
+    const int r = e / NH_, k = e % NH_;
+    const float v = r < NO_ ? params[OW4 + r * NH_ + k] : 0.f;
+    *reinterpret_cast<__nv_bfloat16*>(sm + S_W4 + kmaj(r, k, NH_)) = __float2bfloat16_rn(v);
+  }
+  for (int e = t; e < F_N; e += blockDim.x) {
+    float v = 0.f;
+    if (e < F_B4) v = params[(e < F_B2 ? OB1 + e : e < F_B3 ? OB2 + e - F_B2 : OB3 + e - F_B3)];
+    else if (e < F_MX) v = (e - F_B4) < NO_ ? params[OB4 + e - F_B4] : 0.f;
+    else if (e < F_SX) v = params[NPAR_ + (e - F_MX)];
+    else v = params[NPAR_ + NI_ + (e - F_SX)];
+    fb[e] = v;
+  }
+  const uint32_t mbar = sbase + S_MBAR;
+  if (t == 0) {
+    mbar_init(mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + S_TSLOT),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + S_TSLOT);
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+
+  const uint32_t id64 = idesc_bf16(TILE, NH_), id16 = idesc_bf16(TILE, N4);
+  const uint64_t dA0 = sdesc(sbase + S_A0, 128, (K1 / 8) * 128), dW1 = sdesc(sbase + S_W1, 128, (K1 / 8) * 128);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int64_t ntile = (n + TILE - 1) / TILE;
+  for (int64_t tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+    const int64_t i = tile * TILE + t;
+    /* layer 1 input: normalised features in BF16, K padded with zeros */
+    for (int k = 0; k < K1; k++) {
+      float v = 0.f;
+      if (k < NI_ && i < n) v = (X[i * NI_ + k] - fb[F_MX + k]) / fb[F_SX + k];
+      *reinterpret_cast<__nv_bfloat16*>(sm + S_A0 + kmaj(t, k, K1)) = __float2bfloat16_rn(v);
+    }
+    for (int layer = 0; layer < 4 && ok; layer++) {
+      fence_async_smem();
+      fence_before();
+      __syncthreads();
+      if (t == 0) {
+        fence_after();
+        if (layer == 0) {
+          mma_bf16(tmem, dA0, dW1, id64, 0);
+        } else {
+          const int wo = layer == 1 ? S_W2 : layer == 2 ? S_W3 : S_W4;
+          for (int kk = 0; kk < NH_ / 16; kk++)
+            mma_bf16(tmem, sdesc(sbase + S_A + kk * 256, 128, (NH_ / 8) * 128),
+                     sdesc(sbase + wo + kk * 256, 128, (NH_ / 8) * 128), layer == 3 ? id16 : id64, kk > 0);
+        }
+        mma_commit(mbar);
+      }
+      ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+      phase ^= 1u;
+      if (!ok) break;
+      fence_after();
+      if (layer < 3) {
+        const float* bias = fb + (layer == 0 ? F_B1 : layer == 1 ? F_B2 : F_B3);
+        hidden_epilogue(trow, bias, sm + S_A, t);
+      } else {
+        uint32_t r[16];
+        tmem_ld16(trow, r);
+        tmem_wait_ld();
+        if (i < n) {
+          Y[i * NO_ + 0] = __uint_as_float(r[0]) + fb[F_B4 + 0];
+          Y[i * NO_ + 1] = __uint_as_float(r[1]) + fb[F_B4 + 1];
+        }
+      }
+    }
+    fence_before();
+    __syncthreads();
+  }
+  if (!ok && t == 0) atomicExch(err, 1);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+/* launch over n problems; err: device flag set when a wait gave up */
+int mlp_tc_forward(const float* params, const float* X, float* Y, int64_t n, int* err, cudaStream_t st) {
+  if (n <= 0) return 0;
+  const int64_t ntile = (n + TILE - 1) / TILE;
+  const int grid = (int)(ntile < 152 * 4 ? ntile : 152 * 4);
+  k_mlp_tc<<<grid, 128, S_TOTAL, st>>>(params, X, Y, n, err);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace pgdg

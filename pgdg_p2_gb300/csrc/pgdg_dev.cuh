@@ -247,6 +247,9 @@ void alive_index(const int8_t* phase, unsigned long long* scan, unsigned long lo
                  const unsigned long long* d_n, int64_t cap, int64_t* idx, cudaStream_t st);
 
 /* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls, iterations, cap hits) */
+/* forward pass of the seed surrogate on the tensor cores (k_mlp_tc.cu) */
+int mlp_tc_forward(const float* params, const float* X, float* Y, int64_t n, int* err, cudaStream_t st);
+
 /* scratch of the root partition of a batch (prefix, block sums, order, count) */
 struct PartScratch {
   unsigned long long *pos = nullptr, *blk = nullptr, *dn = nullptr;

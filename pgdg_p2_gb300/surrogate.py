@@ -158,11 +158,13 @@ def baseline_params():
 
 
 class Surrogate:
-    """Device-resident MLP (BF16 weights by default)."""
+    """Device-resident MLP: BF16 weights by default (bf16=False: FP32 weights);
+    tc=True runs forward passes on the tensor cores with BF16 activations."""
 
-    def __init__(self, params=None, bf16=True):
+    def __init__(self, params=None, bf16=True, tc=False):
         self.h = C.c_void_p()
-        M.check(M.lib().pgdg_surrogate_create(1 if bf16 else 0, C.byref(self.h)), "pgdg_surrogate_create")
+        mode = 2 if tc else (1 if bf16 else 0)
+        M.check(M.lib().pgdg_surrogate_create(mode, C.byref(self.h)), "pgdg_surrogate_create")
         self.n = M.lib().pgdg_surrogate_num_params()
         assert self.n == NPARAM + NNORM
         if params is not None:

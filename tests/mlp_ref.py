@@ -70,3 +70,15 @@ def loss_grad(p, X, T, bf16=False):
         g.append(gW.ravel())
         g.append(gb)
     return loss, np.concatenate(g)
+
+
+def forward_bf16_act(p, X):
+    """Forward pass with BF16 weights and BF16 activations (the tensor-core
+    path): normalised inputs and each hidden layer's tanh output are rounded to
+    BF16 before the next layer; sums and biases in FP64."""
+    layers, (mx, sx, _, _) = unpack(p, bf16=True)
+    a = bf16_round(((np.asarray(X, np.float64) - mx) / sx).astype(np.float32)).astype(np.float64)
+    for W, b in layers[:-1]:
+        a = bf16_round(np.tanh(a @ W.T + b).astype(np.float32)).astype(np.float64)
+    W, b = layers[-1]
+    return a @ W.T + b

@@ -412,6 +412,20 @@ def c5_bench(M, S, net, n=1 << 24, reps=3):
     return out
 
 
+def run_c5(args):
+    """Config 5 alone: the batched MGFM micro-benchmark (plain vs learned seed)."""
+    from pgdg_p2_gb300 import mpm as M
+    from pgdg_p2_gb300 import surrogate as S
+    net = S.Surrogate(S.load_default(), tc=True)
+    c5 = c5_bench(M, S, net, n=args.c5_n)
+    print(json.dumps({"metric": "MGFM two-material Riemann problems/s (learned seed, FP64 Newton)",
+                      "value": c5["learned"]["problems_per_s"], "unit": "problems/s", "n_gpus": 1,
+                      "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": f"{args.c5_n} seeded stiffened-gas interface problems (splitmix64 seed 5)"},
+                      "mgfm_c5": c5}), flush=True)
+    net.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -422,10 +436,15 @@ def main():
     ap.add_argument("--no-c5", action="store_true", help="skip the batched MGFM micro-benchmark")
     ap.add_argument("--only-timed", action="store_true", help="timed region only (profiling runs)")
     ap.add_argument("--grid", default="", help="override the grid, e.g. 192,48,48 (profiling runs)")
-    ap.add_argument("--config", type=int, default=3, choices=sorted(WORKLOADS),
-                    help="workload: 1 triple point, 2 cylinder, 3 sphere (default, the metric's), 4 underwater explosion")
+    ap.add_argument("--config", type=int, default=3, choices=sorted(WORKLOADS) + [5],
+                    help="workload: 1 triple point, 2 cylinder, 3 sphere (default, the metric's), 4 underwater "
+                         "explosion, 5 the batched MGFM micro-benchmark alone")
+    ap.add_argument("--c5-n", type=int, default=1 << 24, help="problems of the batched MGFM micro-benchmark")
     args = ap.parse_args()
     global CONFIG_ID, WORKLOAD, GRID, SAMPLE_GRID
+    if args.config == 5:
+        run_c5(args)
+        return
     CONFIG_ID = args.config
     WORKLOAD, GRID, SAMPLE_GRID = WORKLOADS[CONFIG_ID]
     if args.warmup < 3:

@@ -126,16 +126,30 @@ __device__ __forceinline__ float tanh_hw(float x) {
   return y;
 }
 
-/* accumulator row -> bias + tanh -> BF16 row of the next A operand */
+/* two floats -> packed BF16 pair (low half = first) */
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+/* accumulator row -> bias + tanh -> BF16 row of the next A operand; eight
+ * consecutive elements of a row are one 16-byte core-matrix row, stored at once */
 __device__ __forceinline__ void hidden_epilogue(uint32_t trow, const float* bias, unsigned char* sA, int row) {
   for (int c = 0; c < NH_; c += 16) {
     uint32_t r[16];
     tmem_ld16(trow + (uint32_t)c, r);
     tmem_wait_ld();
+    float h[16];
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-      const float h = tanh_hw(__uint_as_float(r[j]) + bias[c + j]);
-      *reinterpret_cast<__nv_bfloat16*>(sA + kmaj(row, c + j, NH_)) = __float2bfloat16_rn(h);
+    for (int j = 0; j < 16; j++) h[j] = tanh_hw(__uint_as_float(r[j]) + bias[c + j]);
+#pragma unroll
+    for (int g = 0; g < 2; g++) {
+      uint4 v;
+      v.x = pack_bf16(h[8 * g + 0], h[8 * g + 1]);
+      v.y = pack_bf16(h[8 * g + 2], h[8 * g + 3]);
+      v.z = pack_bf16(h[8 * g + 4], h[8 * g + 5]);
+      v.w = pack_bf16(h[8 * g + 6], h[8 * g + 7]);
+      *reinterpret_cast<uint4*>(sA + kmaj(row, c + 8 * g, NH_)) = v;
     }
   }
 }
@@ -198,10 +212,19 @@ __global__ void __launch_bounds__(128, 4) k_mlp_tc(const float* __restrict__ par
   for (int64_t tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
     const int64_t i = tile * TILE + t;
     /* layer 1 input: normalised features in BF16, K padded with zeros */
-    for (int k = 0; k < K1; k++) {
-      float v = 0.f;
-      if (k < NI_ && i < n) v = (X[i * NI_ + k] - fb[F_MX + k]) / fb[F_SX + k];
-      *reinterpret_cast<__nv_bfloat16*>(sm + S_A0 + kmaj(t, k, K1)) = __float2bfloat16_rn(v);
+    {
+      float v[K1];
+#pragma unroll
+      for (int k = 0; k < K1; k++) v[k] = (k < NI_ && i < n) ? (X[i * NI_ + k] - fb[F_MX + k]) / fb[F_SX + k] : 0.f;
+#pragma unroll
+      for (int g = 0; g < 2; g++) {
+        uint4 w;
+        w.x = pack_bf16(v[8 * g + 0], v[8 * g + 1]);
+        w.y = pack_bf16(v[8 * g + 2], v[8 * g + 3]);
+        w.z = pack_bf16(v[8 * g + 4], v[8 * g + 5]);
+        w.w = pack_bf16(v[8 * g + 6], v[8 * g + 7]);
+        *reinterpret_cast<uint4*>(sm + S_A0 + kmaj(t, 8 * g, K1)) = w;
+      }
     }
     for (int layer = 0; layer < 4 && ok; layer++) {
       fence_async_smem();

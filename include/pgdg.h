@@ -150,6 +150,15 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
 int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8_t* mat2, const double* gam,
                               const double* pinf, int nmat, int variant, double* out3, int32_t* iters, int64_t n);
 
+/* ---- CUDA graphs of whole steps (no reference counterpart) ----
+ * pgdg_advance replays captured graphs of three steps (one per rotation of
+ * the coordinate buffers) when a step reads nothing back on the host: not at
+ * the first iteration, not while per-method timing or the interface queue is
+ * on, not before the shifting kernel's variant is tuned.  Results equal the
+ * eager steps bit for bit.  on = 0 runs every step eagerly.  Uploads and
+ * changes of surrogate, queue or kernel variant drop the graphs. */
+int pgdg_set_graphs(pgdg_ctx* ctx, int on);
+
 /* ---- kernel variants (no reference counterpart) ----
  * Some kernels have several implementations with identical results; the
  * context times them on its own state at their first call and keeps the

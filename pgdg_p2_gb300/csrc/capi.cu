@@ -31,6 +31,9 @@ struct pgdg_ctx {
   int pst_var = -1;      /* shifting-kernel variant (-1: tune at the next call) */
   int64_t iface_last = 0;
   virtual int iface_download(double*, int8_t*, int64_t, int64_t*) = 0;
+  /* captured step graphs (advance): dropped when what they bake in changes */
+  virtual void invalidate_graphs() = 0;
+  virtual void enable_graphs(bool on) = 0;
   int64_t iterate = 0;
   cudaStream_t st = nullptr;
   virtual int upload_particles(const pgdg_particles*) = 0;
@@ -155,6 +158,7 @@ struct Ctx : pgdg_ctx {
 
   ~Ctx() override {
     if (st) cudaStreamSynchronize(st);
+    drop_graphs();
     for (auto e : ev_pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     part.release();
@@ -391,6 +395,7 @@ struct Ctx : pgdg_ctx {
 
   /* ---------------- exchange ---------------- */
   int upload_particles(const pgdg_particles* pp) override {
+    drop_graphs();
     int64_t n = pp->n;
     if (n > K.cap) {
       err = "particle count exceeds capacity";
@@ -505,6 +510,7 @@ struct Ctx : pgdg_ctx {
 
   /* cell arrays: host element = cell, device component-major over ncell */
   int upload_cells(const pgdg_cells* cc) override {
+    drop_graphs();
     if (cc->n != K.ncell) {
       err = "cell count mismatch";
       return PGDG_EINVAL;
@@ -595,6 +601,7 @@ struct Ctx : pgdg_ctx {
   }
 
   int upload_lists(const int64_t* off, const int64_t* ent) override {
+    drop_graphs();
     std::vector<int64_t> slots;
     int rc = alive_slots(slots);
     if (rc) return rc;
@@ -895,11 +902,91 @@ struct Ctx : pgdg_ctx {
     }
     return PGDG_OK;
   }
-  int advance(int nsteps) override {
-    for (int s = 0; s < nsteps; s++) {
+  /* ---------------- CUDA graphs of whole steps ----------------
+   * A step without the interface queue reads nothing back on the host, so
+   * advance() captures it.  The coordinate buffers rotate with a period of three
+   * steps (the buffer indices are kernel arguments), so the graph holds three
+   * steps, one per rotation phase P.xb.  Steps that cannot be captured run
+   * eagerly: the first iteration (Used_state_update, the particle-based CFL
+   * step), any step while per-method timing or the queue is on, a step before
+   * the kernel-variant tuning, and the remainder of a call below three steps. */
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    int xb_after = 0, hb_after = 0, x0b_after = 0;
+    int64_t launches = 0;
+  };
+  StepGraph graphs[3];
+  bool graphs_enabled = true;
+  void invalidate_graphs() override { drop_graphs(); }
+  void enable_graphs(bool on) override {
+    drop_graphs();
+    graphs_enabled = on;
+  }
+  void drop_graphs() {
+    for (auto& g : graphs) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g = StepGraph{};
+    }
+  }
+  int capture3(StepGraph& sg) {
+    const int xb0 = P.xb, hb0 = P.hb, x0b0 = x0b;
+    const int64_t it0 = iterate, l0 = launches;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PGDG_ECUDA;
+    for (int k = 0; k < 3; k++) {
       set_timestep(nullptr, nullptr);
       iterate++;
       run_step(iterate);
+    }
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    sg.xb_after = P.xb;
+    sg.hb_after = P.hb;
+    sg.x0b_after = x0b;
+    sg.launches = launches - l0;
+    P.xb = xb0;
+    P.hb = hb0;
+    x0b = x0b0;
+    iterate = it0;
+    launches = l0;
+    if (e != cudaSuccess || !g) {
+      cudaGetLastError();
+      return PGDG_ECUDA;
+    }
+    e = cudaGraphInstantiate(&sg.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      sg.exec = nullptr;
+      cudaGetLastError();
+      return PGDG_ECUDA;
+    }
+    return PGDG_OK;
+  }
+  int advance(int nsteps) override {
+    int s = 0;
+    while (s < nsteps) {
+      const bool graphable = graphs_enabled && !prof && !iface_queue && iterate >= 1 && pst_var >= 0 && nsteps - s >= 3;
+      if (graphable) {
+        StepGraph& sg = graphs[P.xb];
+        if (!sg.exec && capture3(sg) != PGDG_OK) {
+          graphs_enabled = false; /* capture refused: stay eager */
+          continue;
+        }
+        if (cudaGraphLaunch(sg.exec, st) != cudaSuccess) {
+          err = "graph launch failed";
+          return PGDG_ECUDA;
+        }
+        P.xb = sg.xb_after;
+        P.hb = sg.hb_after;
+        x0b = sg.x0b_after;
+        iterate += 3;
+        launches += sg.launches;
+        s += 3;
+        continue;
+      }
+      set_timestep(nullptr, nullptr);
+      iterate++;
+      run_step(iterate);
+      s++;
     }
     return PGDG_OK;
   }
@@ -980,6 +1067,11 @@ int pgdg_set_surrogate(pgdg_ctx* ctx, pgdg_mlp* net) {
   }
   ctx->net = (void*)net;
   ctx->iface_queue = net ? 1 : ctx->iface_queue;
+  ctx->invalidate_graphs();
+  return PGDG_OK;
+}
+int pgdg_set_graphs(pgdg_ctx* ctx, int on) {
+  ctx->enable_graphs(on != 0);
   return PGDG_OK;
 }
 int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen) {
@@ -989,6 +1081,7 @@ int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen) {
   }
   if (variant >= 0) ctx->pst_var = variant;
   else if (variant == -1) ctx->pst_var = -1;
+  if (variant >= -1) ctx->invalidate_graphs();
   if (chosen) *chosen = ctx->pst_var;
   return PGDG_OK;
 }
@@ -1002,6 +1095,7 @@ int pgdg_set_iface_queue(pgdg_ctx* ctx, int on) {
     return PGDG_EINVAL;
   }
   ctx->iface_queue = on ? 1 : 0;
+  ctx->invalidate_graphs();
   return PGDG_OK;
 }
 int pgdg_iface_download(pgdg_ctx* ctx, double* in6, int8_t* mat2, int64_t cap, int64_t* n) {

@@ -76,6 +76,7 @@ def lib():
         L.pgdg_set_surrogate.argtypes = [vp, vp]
         L.pgdg_set_iface_queue.argtypes = [vp, C.c_int]
         L.pgdg_tune.argtypes = [vp, C.c_char_p, C.c_int, P(C.c_int)]
+        L.pgdg_set_graphs.argtypes = [vp, C.c_int]
         L.pgdg_iface_download.argtypes = [vp, vp, vp, C.c_int64, P(C.c_int64)]
         _lib = L
     return _lib
@@ -222,6 +223,10 @@ class MPM:
         ch = C.c_int()
         self._ck(lib().pgdg_tune(self.h, kernel.encode(), int(variant), C.byref(ch)), "tune")
         return ch.value
+
+    def set_graphs(self, on):
+        """Replay captured CUDA graphs of whole steps in advance() (default on)."""
+        self._ck(lib().pgdg_set_graphs(self.h, 1 if on else 0), "set_graphs")
 
     def set_iface_queue(self, on):
         """Solve each stage's interface problems as one batch (mixed / FP64_FMA paths)."""

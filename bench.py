@@ -332,8 +332,14 @@ def run_ours(args):
         flops_per = {"pst": N * 137 * 50, "grid_acc": ncell * 13000}.get(dom, 0)
         sm_mhz = peaks.get("sm_max_mhz", 2070.0)
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        # DRAM traffic per shifting launch from the ncu capture of the 192x48x48 case
+        # (433.6 MB read + written for 3,538,944 particles), scaled by the particle
+        # count (the traffic grows with it)
+        traffic = 433.6e6 * N / 3538944 if dom == "pst" and CONFIG_ID == 3 else None
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "peak_source": "measured" if peaks else "fallback",
+                "frac": achieved / hbm, "traffic": traffic, "traffic_note": "bytes per launch, ncu capture of "
+                "the 192x48x48 case scaled by particles" if traffic else None,
+                "peak_source": "measured" if peaks else "fallback",
                 "per_launch_ms": per_launch_ms, "launches": d_cnt,
                 "fp32": {"achieved_tflops": flops_per / (per_launch_ms / 1e3) / 1e12,
                          "nominal_peak_tflops": fp32_peak,

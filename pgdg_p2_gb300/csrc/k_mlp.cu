@@ -5,7 +5,7 @@
  * reference's max(p_l, p_r) (mpm.cpp:893).  The pressure output is a log
  * correction to a closed-form two-shock baseline (mgfm_baseline below); the
  * velocity output is trained with a small weight and does not enter the seed.  The plain Newton solve stays the
- * fallback and the judge: a seeded solve that does not reach |f| <= tol within
+ * fallback and the final check: a seeded solve that does not reach |f| <= tol within
  * the iteration cap is redone from the plain seed, and a problem without a
  * positive root (f(1e-8) < 0) goes straight to the plain solve.
  *

@@ -17,7 +17,7 @@
  * Layer 1's K of 12 is padded to 16 and the output layer's N of 2 to 16 with
  * zero weights.  Against the SIMT forward (FP32 activations, tanhf) the
  * activations here are BF16 (tanh in hardware precision), so outputs differ at
- * the 1e-2 level; the seeded Newton solve judges the seed either way.
+ * the 1e-2 level; the seeded Newton solve checks the seed either way.
  *
  * Waits give up after a fixed number of polls: the kernel then records an
  * error, stops issuing work, frees its tensor memory and returns.

@@ -32,7 +32,7 @@ template <>
 __device__ __forceinline__ float hroot<3, float>(float vol) { return cbrtf(vol) * 3.2f / 2.f; }
 
 template <int D, typename R, bool EX>
-__global__ void __launch_bounds__(128) k_g2p(CaseK K, DevPtrs<R> P, int md, int xs, int x0b, int xn, int hn) {
+__global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPtrs<R> P, int md, int xs, int x0b, int xn, int hn) {
   constexpr int U = D + 2, B = D + 1;
   const int64_t n = (int64_t)P.cnt->n_slots;
   const int64_t nc = K.ncell;
@@ -215,7 +215,7 @@ struct PstSmem {
   unsigned char* ecell; /* cap */
   R* rlo;        /* 2 * nrow */
   R* rhi;        /* 2 * nrow */
-  int lo[3], n[3], nsc, nrow, cap, maxcnt;
+  int lo[3], n[3], nsc, nrow, cap;
 };
 
 template <int D, typename R>
@@ -359,6 +359,77 @@ template <>
 __device__ __forceinline__ int slot_of<float>(float w) { return __float_as_int(w); }
 template <>
 __device__ __forceinline__ int slot_of<double>(double w) { return (int)w; }
+
+/* total order of a staged entry along its row: the row coordinate through an
+ * order-preserving integer image (so NaN and -0 have a place too), ties by slot */
+template <typename R>
+struct RowKey;
+template <>
+struct RowKey<float> {
+  unsigned long long k;
+  __device__ __forceinline__ static RowKey of(const float4& v, int axis) {
+    const float z = axis == 2 ? v.z : v.y;
+    const unsigned hi = (unsigned)fkey(z) ^ 0x80000000u;
+    return RowKey{((unsigned long long)hi << 32) | (unsigned)__float_as_int(v.w)};
+  }
+  __device__ __forceinline__ bool lt(const RowKey& o) const { return k < o.k; }
+};
+template <>
+struct RowKey<double> {
+  long long z;
+  int s;
+  __device__ __forceinline__ static RowKey of(const double4& v, int axis) {
+    const long long i = __double_as_longlong(axis == 2 ? v.z : v.y);
+    return RowKey{i >= 0 ? i : i ^ 0x7FFFFFFFFFFFFFFFLL, (int)v.w};
+  }
+  __device__ __forceinline__ bool lt(const RowKey& o) const { return z < o.z || (z == o.z && s < o.s); }
+};
+
+/* entries a lane holds while its warp merges one row's cell runs; a row of more
+ * than 32x this many entries is sorted by one lane instead */
+constexpr int ROW_SORT_PER_LANE = 4;
+constexpr int SCAN_RED = 66;
+
+/* Block-wide in-place scan of the n counts in a[1..n]: afterwards a[0] = 0 and
+ * a[l + 1] is the sum of counts 0..l.  Each thread scans a contiguous chunk,
+ * warps combine through shuffles and s_red (SCAN_RED ints).  Every thread of the
+ * block calls it; it returns the total to all of them. */
+__device__ __forceinline__ int block_scan_counts(int* a, int n, int* s_red) {
+  const int nt = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5, nw = (nt + 31) >> 5;
+  const int per = (n + nt - 1) / nt;
+  const int l0 = min(t * per, n), l1 = min(l0 + per, n);
+  int s = 0;
+  for (int l = l0; l < l1; l++) s += a[l + 1];
+  int inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) s_red[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    const int v = lane < nw ? s_red[lane] : 0;
+    int iv = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, iv, o);
+      if (lane >= o) iv += y;
+    }
+    s_red[32 + lane] = iv - v;
+    if (lane == 31) s_red[64] = iv;
+  }
+  __syncthreads();
+  int run = s_red[32 + w] + inc - s;
+  for (int l = l0; l < l1; l++) {
+    run += a[l + 1];
+    a[l + 1] = run;
+  }
+  if (t == 0) a[0] = 0;
+  const int total = s_red[64];
+  __syncthreads();
+  return total;
+}
 
 /* one particle: neighbour sum, Bound_pen, Update_PST; sm == nullptr -> global path */
 template <int D, typename R, bool EX, int VAR>
@@ -696,28 +767,17 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
   sm.rlo = reinterpret_cast<R*>(sm.buf + (pst_direct(VAR) && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
   sm.rhi = sm.rlo + 2 * sm.nrow;
   sm.ecell = reinterpret_cast<unsigned char*>(sm.rhi + 2 * sm.nrow);
-  __shared__ int s_total, s_maxcnt;
+  __shared__ int s_red[SCAN_RED];
   for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
     int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
     int64_t c = ((int64_t)(sm.lo[0] + t) * K.N[1] + (sm.lo[1] + s)) * K.N[2] + (sm.lo[2] + m);
     int cnt = min(P.bcnt[c], K.maxpc);
     sm.off[l + 1] = cnt;
-    sm.mid[l] = cnt;
+    if constexpr (EX) sm.mid[l] = cnt;
     sm.bnd[l] = P.boff[c + 1] > P.boff[c] ? 1 : 0;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int mx = 0;
-    sm.off[0] = 0;
-    for (int l = 0; l < sm.nsc; l++) {
-      mx = max(mx, sm.off[l + 1]);
-      sm.off[l + 1] += sm.off[l];
-    }
-    s_total = sm.off[sm.nsc];
-    s_maxcnt = mx;
-  }
-  __syncthreads();
-  sm.maxcnt = s_maxcnt;
+  const int s_total = block_scan_counts(sm.off, sm.nsc, s_red);
   const bool use_sm = s_total <= cap;
   if (use_sm) {
     for (int e = threadIdx.x; e < s_total; e += blockDim.x) {
@@ -745,17 +805,34 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
         v.z = R(0);
       }
       sm.ent[e] = v;
-      if (P.lkey[q] >= KEY_APPEND && (r == 0 || P.lkey[bk[r - 1]] < KEY_APPEND)) sm.mid[l] = r;
+      /* the exact path keeps the reference's list order: binned entries, then
+       * the appended ones (split children) after the boundary particles */
+      if constexpr (EX)
+        if (P.lkey[q] >= KEY_APPEND && (r == 0 || P.lkey[bk[r - 1]] < KEY_APPEND)) sm.mid[l] = r;
     }
     __syncthreads();
+    /* per cell: the exact bounding box of its entries; on the mixed and FMA
+     * paths the cell's entries are also sorted by the row key */
     for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
       R mn[3] = {R(1e30), R(1e30), R(1e30)}, mx[3] = {R(-1e30), R(-1e30), R(-1e30)};
-      for (int e = sm.off[l]; e < sm.off[l + 1]; e++) {
+      const int e0 = sm.off[l], e1 = sm.off[l + 1];
+      for (int e = e0; e < e1; e++) {
         const V4 v = sm.ent[e];
         const R xv[3] = {v.x, v.y, v.z};
         for (int d = 0; d < D; d++) {
           mn[d] = xv[d] < mn[d] ? xv[d] : mn[d];
           mx[d] = xv[d] > mx[d] ? xv[d] : mx[d];
+        }
+        if constexpr (!EX) {
+          const RowKey<R> key = RowKey<R>::of(v, D - 1);
+          int j = e - 1;
+          while (j >= e0) {
+            const V4 u = sm.ent[j];
+            if (RowKey<R>::of(u, D - 1).lt(key)) break;
+            sm.ent[j + 1] = u;
+            j--;
+          }
+          sm.ent[j + 1] = v;
         }
       }
       for (int d = 0; d < D; d++) {
@@ -765,34 +842,84 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
     }
     __syncthreads();
     if constexpr (!EX) {
-      /* one thread per row: tag entries with their cell offset along the row,
-       * insertion-sort them by the row coordinate (ties by slot), and record
-       * the row's bounds in the other axes */
+      /* one warp per row of cells along the last axis: merge the row's sorted
+       * cell runs into one run sorted by the row coordinate (ties by slot), tag
+       * each entry with its cell offset along the row, and record the row's
+       * bounds in the other axes */
       constexpr int RA = D - 1;
       const int nr = sm.n[RA];
-      for (int row = threadIdx.x; row < sm.nrow; row += blockDim.x) {
+      const int lane = threadIdx.x & 31;
+      for (int row = threadIdx.x >> 5; row < sm.nrow; row += blockDim.x >> 5) {
         const int l0 = row * nr;
-        for (int k = 0; k < nr; k++)
-          for (int e = sm.off[l0 + k]; e < sm.off[l0 + k + 1]; e++) sm.ecell[e] = (unsigned char)k;
         const int e0 = sm.off[l0], e1 = sm.off[l0 + nr];
-        for (int i = e0 + 1; i < e1; i++) {
-          const V4 v = sm.ent[i];
-          const unsigned char cv = sm.ecell[i];
-          const R key = (RA == 2) ? v.z : v.y;
-          const int sv = slot_of<R>(v.w);
-          int j = i - 1;
-          while (j >= e0) {
-            const V4 u = sm.ent[j];
-            const R ku = (RA == 2) ? u.z : u.y;
-            if (ku < key || (ku == key && slot_of<R>(u.w) < sv)) break;
-            sm.ent[j + 1] = u;
-            sm.ecell[j + 1] = sm.ecell[j];
-            j--;
+        if (e1 - e0 <= 32 * ROW_SORT_PER_LANE) {
+          /* each lane holds up to ROW_SORT_PER_LANE entries; an entry's place
+           * in the row is its place in its own run plus, for every other run,
+           * the number of that run's keys below its own (both ends first, a
+           * binary search only where the runs overlap) */
+          V4 v[ROW_SORT_PER_LANE];
+          int kc[ROW_SORT_PER_LANE], rk[ROW_SORT_PER_LANE];
+#pragma unroll
+          for (int i = 0; i < ROW_SORT_PER_LANE; i++) {
+            const int e = e0 + lane + 32 * i;
+            kc[i] = -1;
+            rk[i] = 0;
+            if (e < e1) {
+              v[i] = sm.ent[e];
+              int k = 0;
+              while (sm.off[l0 + k + 1] <= e) k++;
+              kc[i] = k;
+              const RowKey<R> key = RowKey<R>::of(v[i], RA);
+              int r = e - sm.off[l0 + k];
+              for (int j = 0; j < nr; j++) {
+                if (j == k) continue;
+                const int a = sm.off[l0 + j], b = sm.off[l0 + j + 1];
+                if (a == b) continue;
+                if (RowKey<R>::of(sm.ent[b - 1], RA).lt(key)) {
+                  r += b - a;
+                  continue;
+                }
+                if (key.lt(RowKey<R>::of(sm.ent[a], RA))) continue;
+                int lo = a, hi = b;
+                while (lo < hi) {
+                  const int md = (lo + hi) >> 1;
+                  if (RowKey<R>::of(sm.ent[md], RA).lt(key)) lo = md + 1;
+                  else hi = md;
+                }
+                r += lo - a;
+              }
+              rk[i] = r;
+            }
           }
-          sm.ent[j + 1] = v;
-          sm.ecell[j + 1] = cv;
+          __syncwarp();
+#pragma unroll
+          for (int i = 0; i < ROW_SORT_PER_LANE; i++)
+            if (kc[i] >= 0) {
+              sm.ent[e0 + rk[i]] = v[i];
+              sm.ecell[e0 + rk[i]] = (unsigned char)kc[i];
+            }
+        } else if (lane == 0) {
+          /* a crowded row: one lane tags and insertion-sorts it */
+          for (int k = 0; k < nr; k++)
+            for (int e = sm.off[l0 + k]; e < sm.off[l0 + k + 1]; e++) sm.ecell[e] = (unsigned char)k;
+          for (int i = e0 + 1; i < e1; i++) {
+            const V4 v = sm.ent[i];
+            const unsigned char cv = sm.ecell[i];
+            const RowKey<R> key = RowKey<R>::of(v, RA);
+            int j = i - 1;
+            while (j >= e0) {
+              const V4 u = sm.ent[j];
+              if (RowKey<R>::of(u, RA).lt(key)) break;
+              sm.ent[j + 1] = u;
+              sm.ecell[j + 1] = sm.ecell[j];
+              j--;
+            }
+            sm.ent[j + 1] = v;
+            sm.ecell[j + 1] = cv;
+          }
         }
-        for (int d = 0; d < D - 1; d++) {
+        if (lane < D - 1) {
+          const int d = lane;
           R a = R(1e30), b = R(-1e30);
           for (int k = 0; k < nr; k++) {
             a = fmin(a, sm.blo[d * sm.nsc + l0 + k]);
@@ -801,6 +928,7 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
           sm.rlo[2 * row + d] = a;
           sm.rhi[2 * row + d] = b;
         }
+        __syncwarp();
       }
       __syncthreads();
     }
@@ -809,26 +937,27 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
   const int nbc = bdim[0] * bdim[1] * bdim[2];
   __shared__ int s_boff[BK::B0 * BK::B1 * BK::B2 + 1];
   __shared__ int s_bcell[BK::B0 * BK::B1 * BK::B2];
-  if (threadIdx.x == 0) {
-    s_boff[0] = 0;
-    for (int q = 0; q < nbc; q++) {
-      int dt0 = q / (bdim[1] * bdim[2]), dt1 = (q / bdim[2]) % bdim[1], dt2 = q % bdim[2];
-      int ci = c0[0] + dt0, cj = c0[1] + dt1, ck = c0[2] + dt2;
-      int cnt = 0;
-      int64_t c = -1;
-      if (ci < K.N[0] && cj < K.N[1] && ck < K.N[2]) {
-        c = ((int64_t)ci * K.N[1] + cj) * K.N[2] + ck;
-        cnt = min(P.bcnt[c], K.maxpc);
-      }
-      s_bcell[q] = (int)c;
-      s_boff[q + 1] = s_boff[q] + cnt;
+  for (int q = threadIdx.x; q < nbc; q += blockDim.x) {
+    int dt0 = q / (bdim[1] * bdim[2]), dt1 = (q / bdim[2]) % bdim[1], dt2 = q % bdim[2];
+    int ci = c0[0] + dt0, cj = c0[1] + dt1, ck = c0[2] + dt2;
+    int cnt = 0;
+    int64_t c = -1;
+    if (ci < K.N[0] && cj < K.N[1] && ck < K.N[2]) {
+      c = ((int64_t)ci * K.N[1] + cj) * K.N[2] + ck;
+      cnt = min(P.bcnt[c], K.maxpc);
     }
+    s_bcell[q] = (int)c;
+    s_boff[q + 1] = cnt;
   }
   __syncthreads();
-  const int npart = s_boff[nbc];
+  const int npart = block_scan_counts(s_boff, nbc, s_red);
   for (int i = threadIdx.x; i < npart; i += blockDim.x) {
-    int q = 0;
-    while (s_boff[q + 1] <= i) q++;
+    int q = 0, qh = nbc - 1; /* the brick cell holding particle i */
+    while (q < qh) {
+      const int md = (q + qh + 1) >> 1;
+      if (s_boff[md] <= i) q = md;
+      else qh = md - 1;
+    }
     const int64_t c = s_bcell[q];
     const int32_t p = P.bucket[c * K.maxpc + (i - s_boff[q])];
     pst_particle<D, R, EX, VAR>(K, P, p, XS, XN, HS, HN, dt, max_v, use_sm ? &sm : nullptr);

@@ -404,7 +404,7 @@ __device__ __forceinline__ R limiter_fn(R ds, int bd_fg) {
 }
 
 template <int D, typename R, bool EX>
-__global__ void __launch_bounds__(128) k_limiter(CaseK K, DevPtrs<R> P) {
+__global__ void __launch_bounds__(128, minblocks_f32<R>(6)) k_limiter(CaseK K, DevPtrs<R> P) {
   constexpr int U = D + 2, B = D + 1, NF = 2 * D;
   const int64_t nc = K.ncell;
   R hps[3], Sax[3];
@@ -605,20 +605,35 @@ struct Prim {
   R P, c, vn;
 };
 
+/* component a of a D-vector held in registers (a select chain: indexing a
+ * register array with a run-time index would move the array to local memory) */
+template <int D, typename R>
+__device__ __forceinline__ R pick(const R* v, int a) {
+  R r = v[0];
+#pragma unroll
+  for (int k = 1; k < D; k++)
+    if (a == k) r = v[k];
+  return r;
+}
+
 /* normal-column flux F[u] = DF[u][a] with DF = U v^T + P I (+ v P in the energy row) */
 template <int D, typename R>
 __device__ __forceinline__ void flux_col(const R* Uu, const R* v, R Pp, int a, R* Fc, R esh) {
   constexpr int U = D + 2;
-  for (int u = 0; u < U; u++) Fc[u] = Uu[u] * v[a];
-  Fc[1 + a] += Pp;
-  Fc[U - 1] += v[a] * Pp;
-  if (esh != R(0)) Fc[U - 1] += v[a] * esh;   /* (E_true + p) v with E_true = E + esh */
+  const R va = pick<D, R>(v, a);
+#pragma unroll
+  for (int u = 0; u < U; u++) Fc[u] = Uu[u] * va;
+#pragma unroll
+  for (int k = 0; k < D; k++)
+    if (k == a) Fc[1 + k] += Pp;
+  Fc[U - 1] += va * Pp;
+  if (esh != R(0)) Fc[U - 1] += va * esh;   /* (E_true + p) v with E_true = E + esh */
 }
 
 /* MODE 0: MGFM solved inline; MODE 2: queue every interface problem (no flux
  * work); MODE 3: read the ghost states of the interface problems from the queue */
 template <int D, typename R, bool EX, int MODE>
-__global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int variant, double voli_d,
+__global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_grid_acc(CaseK K, DevPtrs<R> P, int variant, double voli_d,
                                                  double mij1, double mij2, double mij3, IfaceQ Q) {
   constexpr int U = D + 2, B = D + 1, NF = 2 * D, NQ = (D == 3) ? 4 : 2, NG = (D == 3) ? 8 : 4;
   const int64_t nc = K.ncell;
@@ -698,13 +713,15 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
         else face_rel<D, R>(K, idx, hps, Sax, f, fr);
         const int a = EX ? fc.axis : fr.axis;
         const int fbound = EX ? fc.bound : fr.bound;
-        const int* fnb = EX ? fc.nb : fr.nb;
         const R na = EX ? (R)fc.sgn : fr.sgn;
         R DFn[B][U];
         for (int b = 0; b < B; b++)
           for (int u = 0; u < U; u++) DFn[b][u] = R(0);
         int64_t nb = -1;
-        if (fbound == 0) nb = cidx3(K, fnb[0], fnb[1], fnb[2]);
+        if (fbound == 0) {
+          if constexpr (EX) nb = cidx3(K, fc.nb[0], fc.nb[1], fc.nb[2]);
+          else nb = cidx3(K, fr.nb[0], fr.nb[1], fr.nb[2]);
+        }
         double xn[3] = {0, 0, 0};
         if constexpr (EX)
           if (nb >= 0) center<D>(K, fc.nb, xn);
@@ -732,7 +749,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
           for (int k = 0; k < D; k++) v_i[k] = Ui[1 + k] / rho_i;
           const R P_i = eos_p<R>(E_i - R(0.5) * sq / rho_i, gs, pfe);
           const R c_i = sqrt_r<R>(gs * (pfs + P_i) / rho_i);
-          const R vni = v_i[a] * na;
+          const R vni = pick<D, R>(v_i, a) * na;
           R Fi[U];
           flux_col<D, R>(Ui, v_i, P_i, a, Fi, esh);
           R Nb[B];
@@ -766,7 +783,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
               }
               R rhoe_j = E_j - R(0.5) * sqj * rho_j;
               R P_j = eos_p<R>(rhoe_j, (R)K.gamma[s1], (R)K.pinf_eos[s1]);
-              R vnj = v_j[a] * na;
+              R vnj = pick<D, R>(v_j, a) * na;
               if (ss != s1) {
                 double gh[3];
                 if constexpr (MODE == 2) {
@@ -813,8 +830,8 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
               Ujj[U - 1] = E_j;
               R Fj[U];
               flux_col<D, R>(Ujj, v_j, P_j, a, Fj, esh);
-              const R vni2 = v_i[a] * na;
-              vnj = v_j[a] * na;
+              const R vni2 = pick<D, R>(v_i, a) * na;
+              vnj = pick<D, R>(v_j, a) * na;
               /* HLLC (particle_flow.cpp:232-272) */
               const R SL = amin1(vni2 - c_i, vnj - c_j);
               const R SR = amax1(vni2 + c_i, vnj + c_j);
@@ -849,7 +866,10 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
             }
           } else if (MODE == 2) {
           } else if (fbound == PGDG_BC_WALL) {
-            for (int b = 0; b < B; b++) DFn[b][1 + a] += P_i * Nb[b] * gw;
+            for (int b = 0; b < B; b++)
+#pragma unroll
+              for (int k = 0; k < D; k++)
+                if (k == a) DFn[b][1 + k] += P_i * Nb[b] * gw;
           } else {
             R rho_j = rho_i, P_j = P_i, E_j = E_i;
             R v_j[3], rhov_j[3];
@@ -883,7 +903,7 @@ __global__ void __launch_bounds__(128) k_grid_acc(CaseK K, DevPtrs<R> P, int var
             for (int k = 0; k < D; k++) Uj[1 + k] = rhov_j[k];
             Uj[U - 1] = E_j;
             const R c_j = sqrt_r<R>(gs * (pfs + P_j) / rho_j);
-            const R vnj = v_j[a] * na;
+            const R vnj = pick<D, R>(v_j, a) * na;
             R Fj[U];
             flux_col<D, R>(Uj, v_j, P_j, a, Fj, esh);
             const R SL = amin1(vni - c_i, vnj - c_j);

@@ -262,6 +262,15 @@ int mgfm_seeded_run(void* net, const double* in6, const int8_t* mat2, const doub
                     int variant, double* out3, int32_t* iters, int64_t n, unsigned long long* stats,
                     PartScratch& ps, cudaStream_t st);
 
+/* minimum resident 128-thread blocks per SM asked of the FP32 instantiations of
+ * the per-cell and per-particle kernels (a register cap that trades a few
+ * registers for more warps in flight; these kernels are latency-bound); the
+ * FP64 instantiations keep the compiler's own register count */
+template <typename R>
+__host__ __device__ constexpr int minblocks_f32(int n) {
+  return sizeof(R) == 4 ? n : 1;
+}
+
 /* shared helpers used by several translation units */
 int grid_for(int64_t n, int block);
 void scan_u64(unsigned long long* data, unsigned long long* blk, const unsigned long long* d_n, int64_t cap,

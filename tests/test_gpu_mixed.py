@@ -77,3 +77,41 @@ def test_mixed_shift_vs_oracle(gpu_mod, oracle_mod, cid, grid):
     rel = float(np.abs(sg - so).sum() / max(np.abs(so).sum(), 1e-300))
     print(f"C{cid} shift relative L1 {rel:.3e} over {len(common)} particles")
     assert rel <= TOL_SHIFT, rel
+
+
+# every variant of the shifting kernel sums the same members; all but the
+# warp-cooperative one (1, boundary particles in a second pass) in the same
+# order, so they differ at most by rounding from the order of the boundary sums
+TOL_VARIANTS = 1e-6
+PST_VARIANTS = 6
+
+
+def _shift_after_one_step(M, cs, p, c, prec, variant):
+    g = M.MPM(cs, prec)
+    g.upload_particles(p)
+    g.upload_cells(c)
+    g.tune("pst", variant)
+    g.Set_timestep()
+    g.set_iterate(1)
+    g.MPM_run_simulation(1)
+    g.sync()
+    pg = g.download_particles()
+    order = np.argsort(pg.seq)
+    out = (pg.tv - pg.v)[order, :cs.dim].copy()
+    g.close()
+    return out
+
+
+@pytest.mark.parametrize("cid,grid", [(3, (96, 24, 24)), (1, (112, 48))])
+def test_pst_variants_agree(gpu_mod, cid, grid):
+    M = gpu_mod
+    from pgdg_p2_gb300.abi import PREC_FP64_FMA, PREC_MIXED
+    cs, p, c = M.make_case(cid, grid)
+    for prec in (PREC_MIXED, PREC_FP64_FMA):
+        ref = _shift_after_one_step(M, cs, p, c, prec, 0)
+        scale = max(float(np.abs(ref).sum()), 1e-300)
+        for v in range(1, PST_VARIANTS):
+            s = _shift_after_one_step(M, cs, p, c, prec, v)
+            assert s.shape == ref.shape, (prec, v)
+            rel = float(np.abs(s - ref).sum()) / scale
+            assert rel <= TOL_VARIANTS, (prec, v, rel)

@@ -227,7 +227,7 @@ struct Ctx : pgdg_ctx {
     CK(A(&P.cac, F * nc)); CK(A(&P.calph, F * nc));
     CK(A(&P.ccoef, F * U * B * nc)); CK(A(&P.ccoef0, F * U * B * nc)); CK(A(&P.cdcoef, F * U * B * nc));
     CK(A(&P.clim, F * U * nc)); CK(A(&P.cgv, D * D * nc)); CK(A(&P.cv, D * nc)); CK(A(&P.cP, nc));
-    CK(A(&P.cph, F * nc)); CK(A(&P.cphb, F * nc)); CK(A(&P.cused, nc));
+    CK(A(&P.cph, F * nc)); CK(A(&P.cphb, F * nc)); CK(A(&P.cused, nc)); CK(A(&P.cnew, nc));
     CK(A(&P.bucket, nc * K.maxpc)); CK(A(&P.bcnt, nc)); CK(A(&P.cflag, nc));
     CK(A(&P.dirty_q, nc)); CK(A(&P.flag_q, nc));
     P.qcap = (int64_t)nc;
@@ -782,7 +782,7 @@ struct Ctx : pgdg_ctx {
    * the shifting kernel; nothing to do here */
   int refresh_neighbors() override { return PGDG_OK; }
   int p2g() override {
-    timed("p2g", 1, [&] { Launch<D, R, EX>::p2g(K, P, st); });
+    timed("p2g", 2, [&] { Launch<D, R, EX>::p2g(K, P, st); });
     return PGDG_OK;
   }
   int limiter() override {

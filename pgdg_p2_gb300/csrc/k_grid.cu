@@ -225,139 +225,94 @@ __device__ __forceinline__ R kernel_w_r(R dist, R h, R C) {
   return val;
 }
 
-template <int D, typename R, bool EX>
-__global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
-  constexpr int U = D + 2, B = D + 1, NS = U * D;
-  const int64_t nc = K.ncell;
+/* the P2G neighbourhood of cell ci (its +-1 cells), every particle in it inside
+ * the cut radius, in list order: body(q, ph, xij, ww) with the particle's phase
+ * index, offset from the cell centre and kernel weight times volume */
+template <int D, typename R, typename F_>
+__device__ __forceinline__ void p2g_scan(const CaseK& K, const DevPtrs<R>& P, const int* idx, const double* xc,
+                                         const R* xcr, double Cw, F_&& body) {
   const R* X = P.X[P.xb];
   const double hi = K.p_g * 1 * 3.2 / CUT_OFF;
   const double cut = 1.5 * K.p_sz;
   const float lo2 = (float)(cut * cut * (1.0 - 1e-5)), hi2 = (float)(cut * cut * (1.0 + 1e-5));
+  int lo[3], hi3[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = max(idx[d] - 1, 0);
+    hi3[d] = min(idx[d] + 1, (d < D ? K.N[d] : 1) - 1);
+  }
+  for (int t = lo[0]; t <= hi3[0]; t++)
+    for (int s = lo[1]; s <= hi3[1]; s++)
+      for (int m = lo[2]; m <= hi3[2]; m++) {
+        int64_t cn = cidx3(K, t, s, m);
+        int cntq = min(P.bcnt[cn], K.maxpc);
+        const int32_t* bk = P.bucket + cn * K.maxpc;
+        for (int r = 0; r < cntq; r++) {
+          int32_t q = bk[r];
+          int ph = P.phase[q] - 1;
+          R xij[3];
+          for (int d = 0; d < D; d++) xij[d] = X[d * K.cap + q] - xcr[d];
+          bool in;
+          double dist;
+          if (sizeof(R) == 4) {
+            float dd = 0.f;
+            for (int d = 0; d < D; d++) dd += (float)xij[d] * (float)xij[d];
+            if (dd < lo2) in = true;
+            else if (dd > hi2) in = false;
+            else {
+              double e2 = 0;
+              for (int d = 0; d < D; d++) {
+                double t2 = (double)X[d * K.cap + q] - xc[d];
+                e2 = (d == 0) ? t2 * t2 : e2 + t2 * t2;
+              }
+              in = sqrt(e2) < cut;
+            }
+            dist = (double)sqrtf(dd);
+          } else {
+            double e2 = 0;
+            for (int d = 0; d < D; d++) {
+              double t2 = (double)xij[d];
+              e2 = (d == 0) ? t2 * t2 : e2 + t2 * t2;
+            }
+            dist = sqrt(e2);
+            in = dist < cut;
+          }
+          if (!in) continue;
+          R ww = kernel_w_r<D, R>((R)dist, (R)hi, (R)Cw) * P.vol[q];
+          if (ph < 0 || ph >= F) continue;
+          body(q, ph, xij, ww);
+        }
+      }
+}
+
+/* per cell: the kernel-weighted mass of each phase in the neighbourhood, the
+ * phase flags and volume fractions, and the reset of absent phases; the rare
+ * newly present phases are flagged in cnew for k_p2g_new (a second kernel, so
+ * that this one keeps a small register footprint) */
+template <int D, typename R, bool EX>
+__global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
+  constexpr int U = D + 2, B = D + 1;
+  const int64_t nc = K.ncell;
   GRID_STRIDE(ci, nc) {
-    if (!P.cused[ci]) continue;
+    if (!P.cused[ci]) {
+      P.cnew[ci] = 0;
+      continue;
+    }
     int idx[3];
     cijk<D>(K, ci, idx);
     double xc[3];
     center<D>(K, idx, xc);
     R xcr[3];
     for (int d = 0; d < 3; d++) xcr[d] = (R)xc[d];
-    int lo[3], hi3[3];
-    for (int d = 0; d < 3; d++) {
-      lo[d] = max(idx[d] - 1, 0);
-      hi3[d] = min(idx[d] + 1, (d < D ? K.N[d] : 1) - 1);
-    }
     double mass_t[F] = {0, 0};
+    p2g_scan<D, R>(K, P, idx, xc, xcr, Cw, [&](int32_t, int ph, const R*, R ww) {
+#pragma unroll
+      for (int s = 0; s < F; s++)
+        if (s == ph) mass_t[s] += (double)ww;
+    });
     int newmask = 0;
-    for (int pass = 0; pass < 2; pass++) {
-      double p_avg[U], Cf[NS];
-      int want = -1;
-      if (pass == 1) {
-        for (int s = 0; s < F; s++) {
-          bool ph = mass_t[s] > 0;
-          if (ph && P.cphb[s * nc + ci] == 0) newmask |= 1 << s;
-        }
-        if (!newmask) break;
-        /* newly present phases are rare; sum their averages one phase at a time */
-      }
-      for (int sw = 0; sw < (pass == 0 ? 1 : F); sw++) {
-        if (pass == 1) {
-          if (!(newmask & (1 << sw))) continue;
-          want = sw;
-          for (int u = 0; u < U; u++) p_avg[u] = 0;
-          for (int t = 0; t < NS; t++) Cf[t] = 0;
-        }
-        for (int t = lo[0]; t <= hi3[0]; t++)
-          for (int s = lo[1]; s <= hi3[1]; s++)
-            for (int m = lo[2]; m <= hi3[2]; m++) {
-              int64_t cn = cidx3(K, t, s, m);
-              int cntq = min(P.bcnt[cn], K.maxpc);
-              const int32_t* bk = P.bucket + cn * K.maxpc;
-              for (int r = 0; r < cntq; r++) {
-                int32_t q = bk[r];
-                int ph = P.phase[q] - 1;
-                if (pass == 1 && ph != want) continue;
-                R xij[3];
-                for (int d = 0; d < D; d++) xij[d] = X[d * K.cap + q] - xcr[d];
-                bool in;
-                double dist;
-                if (sizeof(R) == 4) {
-                  float dd = 0.f;
-                  for (int d = 0; d < D; d++) dd += (float)xij[d] * (float)xij[d];
-                  if (dd < lo2) in = true;
-                  else if (dd > hi2) in = false;
-                  else {
-                    double e2 = 0;
-                    for (int d = 0; d < D; d++) {
-                      double t2 = (double)X[d * K.cap + q] - xc[d];
-                      e2 = (d == 0) ? t2 * t2 : e2 + t2 * t2;
-                    }
-                    in = sqrt(e2) < cut;
-                  }
-                  dist = (double)sqrtf(dd);
-                } else {
-                  double e2 = 0;
-                  for (int d = 0; d < D; d++) {
-                    double t2 = (double)xij[d];
-                    e2 = (d == 0) ? t2 * t2 : e2 + t2 * t2;
-                  }
-                  dist = sqrt(e2);
-                  in = dist < cut;
-                }
-                if (!in) continue;
-                R ww = kernel_w_r<D, R>((R)dist, (R)hi, (R)Cw) * P.vol[q];
-                if (ph < 0 || ph >= F) continue;
-                if (pass == 0) {
-                  mass_t[ph] += (double)ww;
-                } else {
-                  double wwd = (double)ww;
-                  double pj[U];
-                  pj[0] = (double)P.rho[q];
-                  for (int k = 0; k < D; k++) pj[1 + k] = (double)P.rhov[k * K.cap + q];
-                  pj[U - 1] = (double)P.E[q];
-                  for (int u = 0; u < U; u++) {
-                    double acc = 0;
-                    for (int b = 0; b < D; b++) {
-                      double sv = (double)P.sl[(u * D + b) * K.cap + q];
-                      acc = (b == 0) ? sv * (-(double)xij[b]) : acc + sv * (-(double)xij[b]);
-                    }
-                    pj[u] += acc;
-                  }
-                  for (int u = 0; u < U; u++) p_avg[u] += pj[u] * wwd;
-                  for (int tt = 0; tt < NS; tt++) Cf[tt] += (double)P.sl[tt * K.cap + q] * wwd;
-                }
-              }
-            }
-        if (pass == 1) {
-          /* initialise the newly present phase (mpm.cpp:345-363) */
-          const int ss = want;
-          const double mt = mass_t[ss] + 1e-20;
-          for (int u = 0; u < U; u++) p_avg[u] /= mt;
-          for (int t = 0; t < NS; t++) Cf[t] /= mt;
-          for (int u = 0; u < U; u++)
-            for (int b = 0; b < B; b++) P.ccoef[((ss * U + u) * B + b) * nc + ci] = R(0);
-          P.ccoef[((ss * U + 0) * B + 0) * nc + ci] = (R)p_avg[0];
-          P.crho[ss * nc + ci] = (R)p_avg[0];
-          for (int k = 0; k < D; k++) {
-            P.ccoef[((ss * U + 1 + k) * B + 0) * nc + ci] = (R)p_avg[1 + k];
-            P.crhov[(ss * D + k) * nc + ci] = (R)p_avg[1 + k];
-          }
-          P.ccoef[((ss * U + U - 1) * B + 0) * nc + ci] = (R)p_avg[U - 1];
-          P.cE[ss * nc + ci] = (R)p_avg[U - 1];
-          for (int u = 0; u < U; u++)
-            for (int b = 0; b < D; b++) P.ccoef[((ss * U + u) * B + 1 + b) * nc + ci] = (R)Cf[u * D + b];
-          R rho = P.crho[ss * nc + ci];
-          R sq = R(0);
-          for (int k = 0; k < D; k++) {
-            R rv = P.crhov[(ss * D + k) * nc + ci];
-            P.cv[k * nc + ci] = rv / rho;
-            sq = (k == 0) ? rv * rv : sq + rv * rv;
-          }
-          R e_j = P.cE[ss * nc + ci] - R(0.5) * sq / rho;
-          P.cP[ci] = eos_p<R>(e_j, (R)K.gamma[ss], (R)K.pinf_eos[ss]);
-          for (int t = 0; t < U * B; t++) P.ccoef0[(ss * U * B + t) * nc + ci] = P.ccoef[(ss * U * B + t) * nc + ci];
-        }
-      }
-    }
+    for (int s = 0; s < F; s++)
+      if (mass_t[s] > 0 && P.cphb[s * nc + ci] == 0) newmask |= 1 << s;
+    P.cnew[ci] = (int8_t)newmask;
     double mass_total = 0;
     for (int t = 0; t < F; t++) mass_total += mass_t[t];
     for (int ss = 0; ss < F; ss++) {
@@ -382,12 +337,83 @@ __global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
   }
 }
 
+/* initialise each newly present phase of a flagged cell (mpm.cpp:345-363) from
+ * the weighted averages of its particles' reconstructed states and slopes; the
+ * phase's mass is summed again over the same particles in the same order, so
+ * it equals k_p2g's bit for bit */
+template <int D, typename R, bool EX>
+__global__ void __launch_bounds__(128) k_p2g_new(CaseK K, DevPtrs<R> P, double Cw) {
+  constexpr int U = D + 2, B = D + 1, NS = U * D;
+  const int64_t nc = K.ncell;
+  GRID_STRIDE(ci, nc) {
+    const int newmask = P.cnew[ci];
+    if (!newmask) continue;
+    int idx[3];
+    cijk<D>(K, ci, idx);
+    double xc[3];
+    center<D>(K, idx, xc);
+    R xcr[3];
+    for (int d = 0; d < 3; d++) xcr[d] = (R)xc[d];
+    for (int ss = 0; ss < F; ss++) {
+      if (!(newmask & (1 << ss))) continue;
+      double p_avg[U], Cf[NS], mt = 0;
+      for (int u = 0; u < U; u++) p_avg[u] = 0;
+      for (int t = 0; t < NS; t++) Cf[t] = 0;
+      p2g_scan<D, R>(K, P, idx, xc, xcr, Cw, [&](int32_t q, int ph, const R* xij, R ww) {
+        if (ph != ss) return;
+        mt += (double)ww;
+        double wwd = (double)ww;
+        double pj[U];
+        pj[0] = (double)P.rho[q];
+        for (int k = 0; k < D; k++) pj[1 + k] = (double)P.rhov[k * K.cap + q];
+        pj[U - 1] = (double)P.E[q];
+        for (int u = 0; u < U; u++) {
+          double acc = 0;
+          for (int b = 0; b < D; b++) {
+            double sv = (double)P.sl[(u * D + b) * K.cap + q];
+            acc = (b == 0) ? sv * (-(double)xij[b]) : acc + sv * (-(double)xij[b]);
+          }
+          pj[u] += acc;
+        }
+        for (int u = 0; u < U; u++) p_avg[u] += pj[u] * wwd;
+        for (int tt = 0; tt < NS; tt++) Cf[tt] += (double)P.sl[tt * K.cap + q] * wwd;
+      });
+      mt += 1e-20;
+      for (int u = 0; u < U; u++) p_avg[u] /= mt;
+      for (int t = 0; t < NS; t++) Cf[t] /= mt;
+      for (int u = 0; u < U; u++)
+        for (int b = 0; b < B; b++) P.ccoef[((ss * U + u) * B + b) * nc + ci] = R(0);
+      P.ccoef[((ss * U + 0) * B + 0) * nc + ci] = (R)p_avg[0];
+      P.crho[ss * nc + ci] = (R)p_avg[0];
+      for (int k = 0; k < D; k++) {
+        P.ccoef[((ss * U + 1 + k) * B + 0) * nc + ci] = (R)p_avg[1 + k];
+        P.crhov[(ss * D + k) * nc + ci] = (R)p_avg[1 + k];
+      }
+      P.ccoef[((ss * U + U - 1) * B + 0) * nc + ci] = (R)p_avg[U - 1];
+      P.cE[ss * nc + ci] = (R)p_avg[U - 1];
+      for (int u = 0; u < U; u++)
+        for (int b = 0; b < D; b++) P.ccoef[((ss * U + u) * B + 1 + b) * nc + ci] = (R)Cf[u * D + b];
+      R rho = P.crho[ss * nc + ci];
+      R sq = R(0);
+      for (int k = 0; k < D; k++) {
+        R rv = P.crhov[(ss * D + k) * nc + ci];
+        P.cv[k * nc + ci] = rv / rho;
+        sq = (k == 0) ? rv * rv : sq + rv * rv;
+      }
+      R e_j = P.cE[ss * nc + ci] - R(0.5) * sq / rho;
+      P.cP[ci] = eos_p<R>(e_j, (R)K.gamma[ss], (R)K.pinf_eos[ss]);
+      for (int t = 0; t < U * B; t++) P.ccoef0[(ss * U * B + t) * nc + ci] = P.ccoef[(ss * U * B + t) * nc + ci];
+    }
+  }
+}
+
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::p2g(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
   const double hi = K.p_g * 1 * 3.2 / CUT_OFF;
   double hh = (D == 2) ? hi * hi : hi * hi * hi;
   double Cw = (D == 2) ? 1.0 / PI_REF / hh * 7. / 4. : 1.0 / PI_REF / hh * 21. / 16.;
   k_p2g<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, Cw);
+  k_p2g_new<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, Cw);
 }
 
 /* ------------------------------------------------------------------ */

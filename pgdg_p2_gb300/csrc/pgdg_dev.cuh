@@ -118,6 +118,7 @@ struct DevPtrs {
   R *cv;                                     /* D */
   R* cP;
   int8_t *cph, *cphb, *cused;                /* F, F, 1 */
+  int8_t* cnew;                              /* P2G: mask of newly present phases */
   int32_t *bucket, *bcnt;
   uint32_t* cflag;  /* bit0 dirty bucket, bit1 flagged (affected neighbourhood) */
   int32_t *dirty_q, *flag_q;

@@ -146,6 +146,7 @@ struct Ctx : pgdg_ctx {
   double* d_tot = nullptr;
   IfaceQ Q{};
   PartScratch part;   /* root partition of the interface batch */
+  unsigned char* pst_scratch = nullptr; /* per-stage row sort of the shifting kernel */
   double *d_gam = nullptr, *d_pinf = nullptr;
   unsigned long long* d_ncell = nullptr;
 
@@ -231,6 +232,7 @@ struct Ctx : pgdg_ctx {
     CK(A(&P.bucket, nc * K.maxpc)); CK(A(&P.bcnt, nc)); CK(A(&P.cflag, nc));
     CK(A(&P.dirty_q, nc)); CK(A(&P.flag_q, nc));
     P.qcap = (int64_t)nc;
+    if (const size_t rsb = Launch<D, R, EX>::pst_scratch_bytes(K)) CK(A(&pst_scratch, rsb));
     CK(A(&P.cnt, 1));
     CK(A(&d_tot, 6));
     /* interface queue: at most 2 phases x 2D faces x 4 points x 1 other phase per cell;
@@ -879,8 +881,9 @@ struct Ctx : pgdg_ctx {
     }
     timed("g2p", 1, [&] { Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, st); });
     if (pst_var < 0)
-      pst_var = tune(Launch<D, R, EX>::pst_variants(), [&](int v) { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, v, st); });
-    timed("pst", 1, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, pst_var, st); });
+      pst_var = tune(Launch<D, R, EX>::pst_variants(),
+                     [&](int v) { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, v, pst_scratch, st); });
+    timed("pst", EX ? 1 : 4, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, pst_var, pst_scratch, st); });
     if (md == 1) timed("store_lists", 2, [&] { Launch<D, R, EX>::store_lists(K, P, xs, hs, xn, st); });
     P.xb = xn;
     P.hb = hn;

@@ -10,6 +10,7 @@
  * which is recomputed on the fly from the stage-start coordinate buffer instead
  * of being stored.
  */
+#include <climits>
 #include <type_traits>
 
 #include "pgdg_dev.cuh"
@@ -199,6 +200,9 @@ struct Vec4<double> {
   using T = double4;
 };
 
+template <typename R>
+struct RowKey;
+
 template <int D, typename R>
 struct PstSmem {
   using V4 = typename Vec4<R>::T;
@@ -209,26 +213,56 @@ struct PstSmem {
   R* bhi;        /* D * nsc */
   V4* ent;       /* cap: (x, y, z | slot) of each staged particle at the stage start */
   unsigned short* buf; /* PST_BUF x PST_THREADS queued member entries */
-  /* mixed / FMA paths: the entries of each row of cells along the last axis
-   * (z in 3D, y in 2D) are sorted by that coordinate; ecell holds each entry's
-   * cell offset along the row, rlo/rhi the row's bounds in the other axes */
+  /* mixed / FMA paths: off holds per staged row (not per cell) the offsets of
+   * its entries, which are sorted by the last-axis coordinate (z in 3D, y in
+   * 2D); ecell holds each entry's cell offset in the row window, rlo/rhi the
+   * row's bounds in the other axes */
   unsigned char* ecell; /* cap */
   R* rlo;        /* 2 * nrow */
   R* rhi;        /* 2 * nrow */
+  long long* rsrc; /* nrow: start of each staged row's range in the row-sorted entries */
   int lo[3], n[3], nsc, nrow, cap;
 };
 
-template <int D, typename R>
-__host__ __device__ inline size_t pst_smem_bytes(int nsc, int nrow, int cap, int qdepth = PST_BUF) {
-  size_t b = sizeof(int) * (size_t)(3 * nsc + 1);
-  b = (b + 31) / 32 * 32;
-  b += sizeof(R) * (size_t)(2 * D * nsc);
-  b = (b + 31) / 32 * 32;
-  b += 4 * sizeof(R) * (size_t)cap;
-  b += sizeof(unsigned short) * (size_t)qdepth * PST_THREADS;
-  b += sizeof(R) * (size_t)(4 * nrow);
-  b += (size_t)cap;
-  return b + 128;
+/* shared-memory layout of one brick; with sm == nullptr only the size */
+template <int D, typename R, bool EX>
+__host__ __device__ inline size_t pst_layout(PstSmem<D, R>* sm, unsigned char* raw, int nsc, int nrow, int cap,
+                                             int qdepth) {
+  using V4 = typename Vec4<R>::T;
+  size_t o = 0;
+  auto take = [&](size_t bytes, size_t align) {
+    o = (o + align - 1) / align * align;
+    const size_t r = o;
+    o += bytes;
+    return r;
+  };
+  const size_t off_o = take(sizeof(int) * (size_t)((nsc > nrow ? nsc : nrow) + 1), 16);
+  const size_t bnd_o = take(sizeof(int) * (size_t)nsc, 16);
+  const size_t mid_o = EX ? take(sizeof(int) * (size_t)nsc, 16) : 0;
+  const size_t blo_o = EX ? take(sizeof(R) * (size_t)(2 * D * nsc), 16) : 0;
+  const size_t ent_o = take(sizeof(V4) * (size_t)cap, 32);
+  const size_t buf_o = take(sizeof(unsigned short) * (size_t)qdepth * PST_THREADS, 16);
+  const size_t rlo_o = EX ? 0 : take(sizeof(R) * (size_t)(4 * nrow), 16);
+  const size_t ec_o = EX ? 0 : take((size_t)cap, 16);
+  const size_t rs_o = EX ? 0 : take(sizeof(long long) * (size_t)nrow, 16);
+  if (sm) {
+    sm->off = reinterpret_cast<int*>(raw + off_o);
+    sm->bnd = reinterpret_cast<int*>(raw + bnd_o);
+    sm->mid = EX ? reinterpret_cast<int*>(raw + mid_o) : nullptr;
+    sm->blo = EX ? reinterpret_cast<R*>(raw + blo_o) : nullptr;
+    sm->bhi = EX ? sm->blo + D * nsc : nullptr;
+    sm->ent = reinterpret_cast<V4*>(raw + ent_o);
+    sm->buf = reinterpret_cast<unsigned short*>(raw + buf_o);
+    sm->rlo = EX ? nullptr : reinterpret_cast<R*>(raw + rlo_o);
+    sm->rhi = EX ? nullptr : sm->rlo + 2 * nrow;
+    sm->ecell = EX ? nullptr : raw + ec_o;
+    sm->rsrc = EX ? nullptr : reinterpret_cast<long long*>(raw + rs_o);
+  }
+  return o + 128;
+}
+template <int D, typename R, bool EX>
+__device__ inline void pst_carve(PstSmem<D, R>& sm, unsigned char* raw, int qdepth) {
+  pst_layout<D, R, EX>(&sm, raw, sm.nsc, sm.nrow, sm.cap, qdepth);
 }
 
 /* per-particle constants and accumulators of the shifting sum */
@@ -359,6 +393,12 @@ template <>
 __device__ __forceinline__ int slot_of<float>(float w) { return __float_as_int(w); }
 template <>
 __device__ __forceinline__ int slot_of<double>(double w) { return (int)w; }
+template <typename R>
+__device__ __forceinline__ R slot_as(int q);
+template <>
+__device__ __forceinline__ float slot_as<float>(int q) { return __int_as_float(q); }
+template <>
+__device__ __forceinline__ double slot_as<double>(int q) { return (double)q; }
 
 /* total order of a staged entry along its row: the row coordinate through an
  * order-preserving integer image (so NaN and -0 have a place too), ties by slot */
@@ -373,6 +413,8 @@ struct RowKey<float> {
     return RowKey{((unsigned long long)hi << 32) | (unsigned)__float_as_int(v.w)};
   }
   __device__ __forceinline__ bool lt(const RowKey& o) const { return k < o.k; }
+  __device__ __forceinline__ static RowKey lowest() { return RowKey{0ull}; }
+  __device__ __forceinline__ static RowKey highest() { return RowKey{~0ull}; }
 };
 template <>
 struct RowKey<double> {
@@ -383,12 +425,182 @@ struct RowKey<double> {
     return RowKey{i >= 0 ? i : i ^ 0x7FFFFFFFFFFFFFFFLL, (int)v.w};
   }
   __device__ __forceinline__ bool lt(const RowKey& o) const { return z < o.z || (z == o.z && s < o.s); }
+  __device__ __forceinline__ static RowKey lowest() { return RowKey{LLONG_MIN, INT_MIN}; }
+  __device__ __forceinline__ static RowKey highest() { return RowKey{LLONG_MAX, INT_MAX}; }
 };
 
-/* entries a lane holds while its warp merges one row's cell runs; a row of more
- * than 32x this many entries is sorted by one lane instead */
-constexpr int ROW_SORT_PER_LANE = 4;
 constexpr int SCAN_RED = 66;
+
+/* ---- rows of cells sorted once per stage (mixed and FMA paths) ----
+ * A row is the line of cells along the last axis (z in 3D, y in 2D).  Each
+ * stage, before the shifting kernel, every row's entries -- (stage-start
+ * position, slot) of the particles binned in its cells -- are sorted by the
+ * last-axis coordinate (ties by slot), in three passes over the cells:
+ *   k_rs_cells  sorts each cell's entries (its run) and records the run's
+ *               smallest and largest key;
+ *   k_rs_rows   per row: offsets of the runs, prefix maxima and suffix minima
+ *               of the run keys;
+ *   k_rs_rank   places each entry at its rank in the row: its place in its
+ *               run, corrected by the runs of the two neighbouring cells; the
+ *               prefix/suffix keys confirm that no run further away
+ *               interleaves, and otherwise every run of the row is counted.
+ * Bricks of the shifting kernel then copy contiguous ranges of sorted rows
+ * instead of sorting their halos.  Layout: fixed maxpc slots per cell, so a
+ * row of NR cells owns NR * maxpc slots of each entry array. */
+template <typename R>
+struct RowSortBufs {
+  typename Vec4<R>::T *run, *row;
+  uint16_t* rk;            /* cell offset in the row of each sorted entry */
+  int32_t *off, *pmin, *pmax;
+  RowKey<R> *kmin, *kmax, *pmaxk, *smink;
+};
+template <typename R>
+struct RowSorted {
+  const typename Vec4<R>::T* row;
+  const uint16_t* rk;
+  const int32_t* pmin;  /* per cell: rank of its first and last entry in its row */
+  const int32_t* pmax;
+};
+template <typename R>
+__host__ __device__ inline size_t rowsort_layout(const CaseK& K, unsigned char* base, RowSortBufs<R>* B) {
+  using V4 = typename Vec4<R>::T;
+  const size_t ne = (size_t)K.ncell * K.maxpc, nc = (size_t)K.ncell;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    o = (o + 255) / 256 * 256;
+    const size_t r = o;
+    o += bytes;
+    return base ? base + r : nullptr;
+  };
+  unsigned char* run = take(ne * sizeof(V4));
+  unsigned char* row = take(ne * sizeof(V4));
+  unsigned char* rk = take(ne * sizeof(uint16_t));
+  unsigned char* off = take(nc * sizeof(int32_t));
+  unsigned char* pmn = take(nc * sizeof(int32_t));
+  unsigned char* pmx = take(nc * sizeof(int32_t));
+  unsigned char* k0 = take(nc * sizeof(RowKey<R>));
+  unsigned char* k1 = take(nc * sizeof(RowKey<R>));
+  unsigned char* k2 = take(nc * sizeof(RowKey<R>));
+  unsigned char* k3 = take(nc * sizeof(RowKey<R>));
+  if (B) {
+    B->run = reinterpret_cast<V4*>(run);
+    B->row = reinterpret_cast<V4*>(row);
+    B->rk = reinterpret_cast<uint16_t*>(rk);
+    B->off = reinterpret_cast<int32_t*>(off);
+    B->pmin = reinterpret_cast<int32_t*>(pmn);
+    B->pmax = reinterpret_cast<int32_t*>(pmx);
+    B->kmin = reinterpret_cast<RowKey<R>*>(k0);
+    B->kmax = reinterpret_cast<RowKey<R>*>(k1);
+    B->pmaxk = reinterpret_cast<RowKey<R>*>(k2);
+    B->smink = reinterpret_cast<RowKey<R>*>(k3);
+  }
+  return o;
+}
+
+template <int D, typename R>
+__global__ void __launch_bounds__(256) k_rs_cells(CaseK K, DevPtrs<R> P, int xs, RowSortBufs<R> B) {
+  using V4 = typename Vec4<R>::T;
+  const R* XS = P.X[xs];
+  GRID_STRIDE(c, K.ncell) {
+    const int cnt = min(P.bcnt[c], K.maxpc);
+    const int64_t base = c * K.maxpc;
+    for (int r = 0; r < cnt; r++) {
+      const int32_t q = P.bucket[base + r];
+      V4 v;
+      v.x = XS[q];
+      v.y = XS[K.cap + q];
+      v.z = (D == 3) ? XS[2 * K.cap + q] : R(0);
+      v.w = slot_as<R>(q);
+      const RowKey<R> key = RowKey<R>::of(v, D - 1);
+      int j = r - 1;
+      while (j >= 0) {
+        const V4 u = B.run[base + j];
+        if (RowKey<R>::of(u, D - 1).lt(key)) break;
+        B.run[base + j + 1] = u;
+        j--;
+      }
+      B.run[base + j + 1] = v;
+    }
+    B.kmin[c] = cnt ? RowKey<R>::of(B.run[base], D - 1) : RowKey<R>::highest();
+    B.kmax[c] = cnt ? RowKey<R>::of(B.run[base + cnt - 1], D - 1) : RowKey<R>::lowest();
+  }
+}
+
+template <int D, typename R>
+__global__ void __launch_bounds__(128) k_rs_rows(CaseK K, DevPtrs<R> P, RowSortBufs<R> B) {
+  const int NR = K.N[D - 1];
+  const int64_t nrows = K.ncell / NR;
+  GRID_STRIDE(rw, nrows) {
+    const int64_t c0 = rw * NR;
+    int acc = 0;
+    RowKey<R> mx = RowKey<R>::lowest();
+    for (int k = 0; k < NR; k++) {
+      const int64_t c = c0 + k;
+      B.off[c] = acc;
+      acc += min(P.bcnt[c], K.maxpc);
+      const RowKey<R> km = B.kmax[c];
+      if (mx.lt(km)) mx = km;
+      B.pmaxk[c] = mx;
+      B.pmin[c] = INT_MAX;
+      B.pmax[c] = -1;
+    }
+    RowKey<R> mn = RowKey<R>::highest();
+    for (int k = NR - 1; k >= 0; k--) {
+      const int64_t c = c0 + k;
+      const RowKey<R> km = B.kmin[c];
+      if (km.lt(mn)) mn = km;
+      B.smink[c] = mn;
+    }
+  }
+}
+
+/* entries of cell c's sorted run whose key is below key */
+template <int D, typename R>
+__device__ __forceinline__ int rs_count_less(const CaseK& K, const DevPtrs<R>& P, const RowSortBufs<R>& B, int64_t c,
+                                             const RowKey<R>& key) {
+  const int cnt = min(P.bcnt[c], K.maxpc);
+  if (!cnt || key.lt(B.kmin[c])) return 0;
+  if (B.kmax[c].lt(key)) return cnt;
+  const int64_t base = c * K.maxpc;
+  int lo = 0, hi = cnt;
+  while (lo < hi) {
+    const int md = (lo + hi) >> 1;
+    if (RowKey<R>::of(B.run[base + md], D - 1).lt(key)) lo = md + 1;
+    else hi = md;
+  }
+  return lo;
+}
+
+template <int D, typename R>
+__global__ void __launch_bounds__(256) k_rs_rank(CaseK K, DevPtrs<R> P, RowSortBufs<R> B) {
+  using V4 = typename Vec4<R>::T;
+  const int NR = K.N[D - 1];
+  GRID_STRIDE(c, K.ncell) {
+    const int cnt = min(P.bcnt[c], K.maxpc);
+    if (!cnt) continue;
+    const int64_t rw = c / NR;
+    const int k = (int)(c - rw * NR);
+    const int64_t base = c * K.maxpc, RB = rw * NR * K.maxpc;
+    const int off_c = B.off[c];
+    for (int r = 0; r < cnt; r++) {
+      const V4 v = B.run[base + r];
+      const RowKey<R> key = RowKey<R>::of(v, D - 1);
+      int rank = off_c + r;
+      if (k >= 1) rank -= min(P.bcnt[c - 1], K.maxpc) - rs_count_less<D, R>(K, P, B, c - 1, key);
+      if (k + 1 < NR) rank += rs_count_less<D, R>(K, P, B, c + 1, key);
+      const bool far_ok = (k < 2 || B.pmaxk[c - 2].lt(key)) && (k + 2 >= NR || key.lt(B.smink[c + 2]));
+      if (!far_ok) {
+        rank = r;
+        for (int j = 0; j < NR; j++)
+          if (j != k) rank += rs_count_less<D, R>(K, P, B, rw * NR + j, key);
+      }
+      B.row[RB + rank] = v;
+      B.rk[RB + rank] = (uint16_t)k;
+      if (r == 0) B.pmin[c] = rank;
+      if (r == cnt - 1) B.pmax[c] = rank;
+    }
+  }
+}
 
 /* Block-wide in-place scan of the n counts in a[1..n]: afterwards a[0] = 0 and
  * a[l + 1] is the sum of counts 0..l.  Each thread scans a contiguous chunk,
@@ -517,8 +729,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
           if (dxy <= lim2m) {
             const R w = sqrt_r<R>(lim2m - dxy); /* half chord of the 2h sphere */
             const R za = zp - w, zb = zp + w;
-            const int rl = row * sm->n[RA];
-            int e = sm->off[rl], hi_e = sm->off[rl + sm->n[RA]];
+            int e = sm->off[row], hi_e = sm->off[row + 1];
             const int e1 = hi_e;
             while (e < hi_e) { /* first entry with coordinate >= za */
               const int m = (e + hi_e) >> 1;
@@ -584,8 +795,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
           }
           if (!__any_sync(am, need)) continue;
           const float fa = warp_min_lo(am, za), fb = warp_max_hi(am, zb);
-          const int rl = row * sm->n[RA];
-          int e = sm->off[rl], hi_e = sm->off[rl + sm->n[RA]];
+          int e = sm->off[row], hi_e = sm->off[row + 1];
           const int e1 = hi_e;
           while (e < hi_e) { /* first entry with coordinate >= the union's lower end */
             const int m = (e + hi_e) >> 1;
@@ -724,7 +934,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
 
 template <int D, typename R, bool EX, int VAR>
 __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn,
-                                                    int nb0, int nb1, int cap) {
+                                                    int nb0, int nb1, int cap, RowSorted<R> RS) {
   using BK = BrickOf<D, VAR>;
   using V4 = typename Vec4<R>::T;
   extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -752,183 +962,130 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
   }
   sm.nsc = sm.n[0] * sm.n[1] * sm.n[2];
   sm.cap = cap;
-  sm.off = reinterpret_cast<int*>(smem_raw);
-  sm.mid = sm.off + sm.nsc + 1;
-  sm.bnd = sm.mid + sm.nsc;
-  size_t o = sizeof(int) * (size_t)(3 * sm.nsc + 1);
-  o = (o + 31) / 32 * 32;
-  sm.blo = reinterpret_cast<R*>(smem_raw + o);
-  sm.bhi = sm.blo + D * sm.nsc;
-  o += sizeof(R) * (size_t)(2 * D * sm.nsc);
-  o = (o + 31) / 32 * 32;
-  sm.ent = reinterpret_cast<V4*>(smem_raw + o);
-  sm.buf = reinterpret_cast<unsigned short*>(sm.ent + cap);
   sm.nrow = (D == 3) ? sm.n[0] * sm.n[1] : sm.n[0];
-  sm.rlo = reinterpret_cast<R*>(sm.buf + (pst_direct(VAR) && !EX ? (size_t)0 : (size_t)PST_BUF * PST_THREADS));
-  sm.rhi = sm.rlo + 2 * sm.nrow;
-  sm.ecell = reinterpret_cast<unsigned char*>(sm.rhi + 2 * sm.nrow);
+  pst_carve<D, R, EX>(sm, smem_raw, (!EX && pst_direct(VAR)) ? 0 : PST_BUF);
   __shared__ int s_red[SCAN_RED];
-  for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
-    int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
-    int64_t c = ((int64_t)(sm.lo[0] + t) * K.N[1] + (sm.lo[1] + s)) * K.N[2] + (sm.lo[2] + m);
-    int cnt = min(P.bcnt[c], K.maxpc);
-    sm.off[l + 1] = cnt;
-    if constexpr (EX) sm.mid[l] = cnt;
-    sm.bnd[l] = P.boff[c + 1] > P.boff[c] ? 1 : 0;
-  }
-  __syncthreads();
-  const int s_total = block_scan_counts(sm.off, sm.nsc, s_red);
-  const bool use_sm = s_total <= cap;
-  if (use_sm) {
-    for (int e = threadIdx.x; e < s_total; e += blockDim.x) {
-      int lo = 0, hi = sm.nsc - 1;
-      while (lo < hi) {
-        int md = (lo + hi + 1) >> 1;
-        if (sm.off[md] <= e) lo = md;
-        else hi = md - 1;
-      }
-      const int l = lo, r = e - sm.off[l];
+  int s_total;
+  if constexpr (EX) {
+    for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
       int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
       int64_t c = ((int64_t)(sm.lo[0] + t) * K.N[1] + (sm.lo[1] + s)) * K.N[2] + (sm.lo[2] + m);
-      const int32_t* bk = P.bucket + c * K.maxpc;
-      int32_t q = bk[r];
-      V4 v;
-      v.x = XS[q];
-      v.y = XS[K.cap + q];
-      if constexpr (D == 3) {
-        v.z = XS[2 * K.cap + q];
-        if constexpr (sizeof(R) == 4) v.w = __int_as_float(q);
-        else v.w = (R)q;
-      } else {
-        if constexpr (sizeof(R) == 4) v.w = __int_as_float(q);
-        else v.w = (R)q;
-        v.z = R(0);
-      }
-      sm.ent[e] = v;
-      /* the exact path keeps the reference's list order: binned entries, then
-       * the appended ones (split children) after the boundary particles */
-      if constexpr (EX)
-        if (P.lkey[q] >= KEY_APPEND && (r == 0 || P.lkey[bk[r - 1]] < KEY_APPEND)) sm.mid[l] = r;
+      int cnt = min(P.bcnt[c], K.maxpc);
+      sm.off[l + 1] = cnt;
+      sm.mid[l] = cnt;
+      sm.bnd[l] = P.boff[c + 1] > P.boff[c] ? 1 : 0;
     }
     __syncthreads();
-    /* per cell: the exact bounding box of its entries; on the mixed and FMA
-     * paths the cell's entries are also sorted by the row key */
+    s_total = block_scan_counts(sm.off, sm.nsc, s_red);
+  } else {
+    /* boundary-particle flag of each staged cell, and per staged row the range
+     * of the stage's row-sorted entries that holds every entry of the row's
+     * window cells (entries of other cells of the row can lie inside the range
+     * where they drifted across a window end; their tag excludes them) */
     for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
-      R mn[3] = {R(1e30), R(1e30), R(1e30)}, mx[3] = {R(-1e30), R(-1e30), R(-1e30)};
-      const int e0 = sm.off[l], e1 = sm.off[l + 1];
-      for (int e = e0; e < e1; e++) {
-        const V4 v = sm.ent[e];
-        const R xv[3] = {v.x, v.y, v.z};
-        for (int d = 0; d < D; d++) {
-          mn[d] = xv[d] < mn[d] ? xv[d] : mn[d];
-          mx[d] = xv[d] > mx[d] ? xv[d] : mx[d];
-        }
-        if constexpr (!EX) {
-          const RowKey<R> key = RowKey<R>::of(v, D - 1);
-          int j = e - 1;
-          while (j >= e0) {
-            const V4 u = sm.ent[j];
-            if (RowKey<R>::of(u, D - 1).lt(key)) break;
-            sm.ent[j + 1] = u;
-            j--;
-          }
-          sm.ent[j + 1] = v;
-        }
+      int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
+      int64_t c = ((int64_t)(sm.lo[0] + t) * K.N[1] + (sm.lo[1] + s)) * K.N[2] + (sm.lo[2] + m);
+      sm.bnd[l] = P.boff[c + 1] > P.boff[c] ? 1 : 0;
+    }
+    constexpr int RA = D - 1;
+    const int NR = K.N[RA];
+    for (int row = threadIdx.x; row < sm.nrow; row += blockDim.x) {
+      const int64_t gr = (D == 3) ? (int64_t)(sm.lo[0] + row / sm.n[1]) * K.N[1] + (sm.lo[1] + row % sm.n[1])
+                                  : (int64_t)(sm.lo[0] + row);
+      int first = INT_MAX, last = -1;
+      for (int k = 0; k < sm.n[RA]; k++) {
+        const int64_t c = gr * NR + sm.lo[RA] + k;
+        first = min(first, RS.pmin[c]);
+        last = max(last, RS.pmax[c]);
       }
-      for (int d = 0; d < D; d++) {
-        sm.blo[d * sm.nsc + l] = mn[d];
-        sm.bhi[d * sm.nsc + l] = mx[d];
-      }
+      sm.off[row + 1] = last >= first ? last - first + 1 : 0;
+      sm.rsrc[row] = gr * NR * K.maxpc + (last >= first ? first : 0);
     }
     __syncthreads();
-    if constexpr (!EX) {
-      /* one warp per row of cells along the last axis: merge the row's sorted
-       * cell runs into one run sorted by the row coordinate (ties by slot), tag
-       * each entry with its cell offset along the row, and record the row's
-       * bounds in the other axes */
+    s_total = block_scan_counts(sm.off, sm.nrow, s_red);
+  }
+  const bool use_sm = s_total <= cap;
+  if (use_sm) {
+    if constexpr (EX) {
+      /* slots: one thread per staged cell copies its list into the entry
+       * slots and finds the first appended entry (the reference's list order
+       * puts the appended split children after the boundary particles) */
+      for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
+        const int t = l / (sm.n[1] * sm.n[2]), s = (l / sm.n[2]) % sm.n[1], m = l % sm.n[2];
+        const int64_t c = ((int64_t)(sm.lo[0] + t) * K.N[1] + (sm.lo[1] + s)) * K.N[2] + (sm.lo[2] + m);
+        const int32_t* bk = P.bucket + c * K.maxpc;
+        const int e0 = sm.off[l], cnt = sm.off[l + 1] - e0;
+        bool app = false;
+        for (int r = 0; r < cnt; r++) {
+          const int32_t q = bk[r];
+          sm.ent[e0 + r].w = slot_as<R>(q);
+          if (!app && P.lkey[q] >= KEY_APPEND) {
+            sm.mid[l] = r;
+            app = true;
+          }
+        }
+      }
+      __syncthreads();
+      /* stage-start coordinates: one thread per entry */
+      for (int e = threadIdx.x; e < s_total; e += blockDim.x) {
+        V4 v = sm.ent[e];
+        const int32_t q = slot_of<R>(v.w);
+        v.x = XS[q];
+        v.y = XS[K.cap + q];
+        v.z = (D == 3) ? XS[2 * K.cap + q] : R(0);
+        sm.ent[e] = v;
+      }
+      __syncthreads();
+      /* per cell: the exact bounding box of its entries */
+      for (int l = threadIdx.x; l < sm.nsc; l += blockDim.x) {
+        R mn[3] = {R(1e30), R(1e30), R(1e30)}, mx[3] = {R(-1e30), R(-1e30), R(-1e30)};
+        for (int e = sm.off[l]; e < sm.off[l + 1]; e++) {
+          const V4 v = sm.ent[e];
+          const R xv[3] = {v.x, v.y, v.z};
+          for (int d = 0; d < D; d++) {
+            mn[d] = xv[d] < mn[d] ? xv[d] : mn[d];
+            mx[d] = xv[d] > mx[d] ? xv[d] : mx[d];
+          }
+        }
+        for (int d = 0; d < D; d++) {
+          sm.blo[d * sm.nsc + l] = mn[d];
+          sm.bhi[d * sm.nsc + l] = mx[d];
+        }
+      }
+      __syncthreads();
+    } else {
+      /* one warp per staged row copies its range (coalesced), tags each entry
+       * with its cell's offset in the row window (255 outside the window) and
+       * reduces the row's bounds in the other axes */
       constexpr int RA = D - 1;
-      const int nr = sm.n[RA];
       const int lane = threadIdx.x & 31;
       for (int row = threadIdx.x >> 5; row < sm.nrow; row += blockDim.x >> 5) {
-        const int l0 = row * nr;
-        const int e0 = sm.off[l0], e1 = sm.off[l0 + nr];
-        if (e1 - e0 <= 32 * ROW_SORT_PER_LANE) {
-          /* each lane holds up to ROW_SORT_PER_LANE entries; an entry's place
-           * in the row is its place in its own run plus, for every other run,
-           * the number of that run's keys below its own (both ends first, a
-           * binary search only where the runs overlap) */
-          V4 v[ROW_SORT_PER_LANE];
-          int kc[ROW_SORT_PER_LANE], rk[ROW_SORT_PER_LANE];
-#pragma unroll
-          for (int i = 0; i < ROW_SORT_PER_LANE; i++) {
-            const int e = e0 + lane + 32 * i;
-            kc[i] = -1;
-            rk[i] = 0;
-            if (e < e1) {
-              v[i] = sm.ent[e];
-              int k = 0;
-              while (sm.off[l0 + k + 1] <= e) k++;
-              kc[i] = k;
-              const RowKey<R> key = RowKey<R>::of(v[i], RA);
-              int r = e - sm.off[l0 + k];
-              for (int j = 0; j < nr; j++) {
-                if (j == k) continue;
-                const int a = sm.off[l0 + j], b = sm.off[l0 + j + 1];
-                if (a == b) continue;
-                if (RowKey<R>::of(sm.ent[b - 1], RA).lt(key)) {
-                  r += b - a;
-                  continue;
-                }
-                if (key.lt(RowKey<R>::of(sm.ent[a], RA))) continue;
-                int lo = a, hi = b;
-                while (lo < hi) {
-                  const int md = (lo + hi) >> 1;
-                  if (RowKey<R>::of(sm.ent[md], RA).lt(key)) lo = md + 1;
-                  else hi = md;
-                }
-                r += lo - a;
-              }
-              rk[i] = r;
-            }
+        const int e0 = sm.off[row], len = sm.off[row + 1] - e0;
+        const int64_t src = sm.rsrc[row];
+        R mn[2] = {R(1e30), R(1e30)}, mx[2] = {R(-1e30), R(-1e30)};
+        for (int i = lane; i < len; i += 32) {
+          const V4 v = RS.row[src + i];
+          const int kk = (int)RS.rk[src + i] - sm.lo[RA];
+          sm.ent[e0 + i] = v;
+          sm.ecell[e0 + i] = (unsigned char)((kk >= 0 && kk < sm.n[RA]) ? kk : 255);
+          const R xv[2] = {v.x, v.y};
+          for (int d = 0; d < D - 1; d++) {
+            mn[d] = xv[d] < mn[d] ? xv[d] : mn[d];
+            mx[d] = xv[d] > mx[d] ? xv[d] : mx[d];
           }
-          __syncwarp();
+        }
+        for (int d = 0; d < D - 1; d++) {
 #pragma unroll
-          for (int i = 0; i < ROW_SORT_PER_LANE; i++)
-            if (kc[i] >= 0) {
-              sm.ent[e0 + rk[i]] = v[i];
-              sm.ecell[e0 + rk[i]] = (unsigned char)kc[i];
-            }
-        } else if (lane == 0) {
-          /* a crowded row: one lane tags and insertion-sorts it */
-          for (int k = 0; k < nr; k++)
-            for (int e = sm.off[l0 + k]; e < sm.off[l0 + k + 1]; e++) sm.ecell[e] = (unsigned char)k;
-          for (int i = e0 + 1; i < e1; i++) {
-            const V4 v = sm.ent[i];
-            const unsigned char cv = sm.ecell[i];
-            const RowKey<R> key = RowKey<R>::of(v, RA);
-            int j = i - 1;
-            while (j >= e0) {
-              const V4 u = sm.ent[j];
-              if (RowKey<R>::of(u, RA).lt(key)) break;
-              sm.ent[j + 1] = u;
-              sm.ecell[j + 1] = sm.ecell[j];
-              j--;
-            }
-            sm.ent[j + 1] = v;
-            sm.ecell[j + 1] = cv;
+          for (int o = 16; o > 0; o >>= 1) {
+            const R a = __shfl_xor_sync(0xffffffffu, mn[d], o), b = __shfl_xor_sync(0xffffffffu, mx[d], o);
+            mn[d] = a < mn[d] ? a : mn[d];
+            mx[d] = b > mx[d] ? b : mx[d];
           }
         }
         if (lane < D - 1) {
-          const int d = lane;
-          R a = R(1e30), b = R(-1e30);
-          for (int k = 0; k < nr; k++) {
-            a = fmin(a, sm.blo[d * sm.nsc + l0 + k]);
-            b = fmax(b, sm.bhi[d * sm.nsc + l0 + k]);
-          }
-          sm.rlo[2 * row + d] = a;
-          sm.rhi[2 * row + d] = b;
+          sm.rlo[2 * row + lane] = lane == 0 ? mn[0] : mn[1];
+          sm.rhi[2 * row + lane] = lane == 0 ? mx[0] : mx[1];
         }
-        __syncwarp();
       }
       __syncthreads();
     }
@@ -965,7 +1122,8 @@ __global__ void __launch_bounds__(pst_threads(VAR), pst_minblocks(VAR)) k_pst(Ca
 }
 
 template <int D, typename R, bool EX, int VAR>
-static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, cudaStream_t st) {
+static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, const RowSorted<R>& RS,
+                       cudaStream_t st) {
   using BK = BrickOf<D, VAR>;
   const int nb0 = (D == 3) ? (K.N[2] + BK::B2 - 1) / BK::B2 : 1;
   const int nb1 = (K.N[1] + BK::B1 - 1) / BK::B1;
@@ -979,17 +1137,17 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
    * it at 1/8 so three blocks fit in an SM's shared memory */
   int cap = (!EX && (VAR == 3 || VAR >= 5)) ? nsc * ppc * 9 / 8 : nsc * ppc * 5 / 4;
   if (cap > 65535) cap = 65535;
-  size_t bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, qdepth);
+  size_t bytes = pst_layout<D, R, EX>(nullptr, nullptr, nsc, nrow, cap, qdepth);
   while (bytes > 220 * 1024 && cap > 256) {
     cap = cap * 3 / 4;
-    bytes = pst_smem_bytes<D, R>(nsc, nrow, cap, qdepth);
+    bytes = pst_layout<D, R, EX>(nullptr, nullptr, nsc, nrow, cap, qdepth);
   }
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_pst<D, R, EX, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 224 * 1024);
     attr_set = true;
   }
-  k_pst<D, R, EX, VAR><<<nbx * nb1 * nb0, pst_threads(VAR), bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap);
+  k_pst<D, R, EX, VAR><<<nbx * nb1 * nb0, pst_threads(VAR), bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap, RS);
 }
 
 /* variants of the shifting kernel (identical results; the context's autotuner
@@ -1003,24 +1161,41 @@ int Launch<D, R, EX>::pst_variants() {
   return EX ? 1 : 6;
 }
 
+/* device scratch of the per-stage row sort (0 on the exact path) */
+template <int D, typename R, bool EX>
+size_t Launch<D, R, EX>::pst_scratch_bytes(const CaseK& K) {
+  return EX ? 0 : rowsort_layout<R>(K, nullptr, nullptr);
+}
+
+/* launches: the exact path 1; otherwise the three row-sort passes and the
+ * shifting kernel (4) */
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, int var,
-                           cudaStream_t st) {
+                           void* scratch, cudaStream_t st) {
   if constexpr (EX) {
-    pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, st);
+    pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, RowSorted<R>{}, st);
   } else {
-    if (var == 1) pst_launch<D, R, EX, 1>(K, P, xs, hs, xn, hn, st);
-    else if (var == 2) pst_launch<D, R, EX, 2>(K, P, xs, hs, xn, hn, st);
-    else if (var == 3) pst_launch<D, R, EX, 3>(K, P, xs, hs, xn, hn, st);
-    else if (var == 4) pst_launch<D, R, EX, 5>(K, P, xs, hs, xn, hn, st);
-    else if (var == 5) pst_launch<D, R, EX, 6>(K, P, xs, hs, xn, hn, st);
-    else pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, st);
+    RowSortBufs<R> B;
+    rowsort_layout<R>(K, static_cast<unsigned char*>(scratch), &B);
+    const int64_t nrows = K.ncell / K.N[D - 1];
+    k_rs_cells<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, xs, B);
+    k_rs_rows<D, R><<<grid_for(nrows, 128), 128, 0, st>>>(K, P, B);
+    k_rs_rank<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, B);
+    const RowSorted<R> RS{B.row, B.rk, B.pmin, B.pmax};
+    if (var == 1) pst_launch<D, R, EX, 1>(K, P, xs, hs, xn, hn, RS, st);
+    else if (var == 2) pst_launch<D, R, EX, 2>(K, P, xs, hs, xn, hn, RS, st);
+    else if (var == 3) pst_launch<D, R, EX, 3>(K, P, xs, hs, xn, hn, RS, st);
+    else if (var == 4) pst_launch<D, R, EX, 5>(K, P, xs, hs, xn, hn, RS, st);
+    else if (var == 5) pst_launch<D, R, EX, 6>(K, P, xs, hs, xn, hn, RS, st);
+    else pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, RS, st);
   }
 }
 
 #define PGDG_INST(D, R, EX)                                                                              \
   template void Launch<D, R, EX>::g2p(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, cudaStream_t); \
-  template void Launch<D, R, EX>::pst(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, cudaStream_t); \
+  template void Launch<D, R, EX>::pst(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, void*,        \
+                                      cudaStream_t);                                                       \
+  template size_t Launch<D, R, EX>::pst_scratch_bytes(const CaseK&);                                       \
   template int Launch<D, R, EX>::pst_variants();
 #ifdef PGDG_EXACT_TU
 PGDG_INST(2, double, true)

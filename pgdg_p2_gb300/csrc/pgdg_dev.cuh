@@ -211,7 +211,10 @@ struct Launch {
   /* xs/hs: stage-start coordinate/h buffers, x0: step-start coordinates (md 1),
    * xn/hn: buffers receiving the new coordinates/h */
   static void g2p(const CaseK&, const DevPtrs<R>&, int md, int xs, int x0, int xn, int hn, cudaStream_t);
-  static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, int var, cudaStream_t);
+  /* shifting: scratch holds pst_scratch_bytes(K) bytes of device memory */
+  static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, int var, void* scratch,
+                  cudaStream_t);
+  static size_t pst_scratch_bytes(const CaseK&);
   static int pst_variants();
 };
 

@@ -215,7 +215,7 @@ struct Ctx : pgdg_ctx {
     CK(A(&P.c, n)); CK(A(&P.P, n));
     CK(A(&P.rhov, D * n)); CK(A(&P.v, D * n)); CK(A(&P.tv, D * n));
     CK(A(&P.sl, NS * n));
-    CK(A(&P.rec, 8 * n));
+    CK(A(&P.rec, 4 * n)); CK(A(&P.rec2, 2 * n));
     CK(A(&P.phase, n)); CK(A(&P.mark_in, n)); CK(A(&P.seq, n));
     CK(A(&P.lcell, n)); CK(A(&P.lkey, n)); CK(A(&P.list_len, n)); CK(A(&P.list_off, n));
     CK(A(&P.target, n)); CK(A(&P.aff, n)); CK(A(&P.mflag, n)); CK(A(&P.evcode, n));

@@ -18,6 +18,28 @@
 namespace pgdg {
 
 constexpr int BLK = 256;
+
+/* 16- and 8-byte (FP32) or 32- and 16-byte (FP64) vector of R */
+template <typename R>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  using T = float4;
+};
+template <>
+struct Vec4<double> {
+  using T = double4;
+};
+template <typename R>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  using T = float2;
+};
+template <>
+struct Vec2<double> {
+  using T = double2;
+};
 #define GRID_STRIDE(i, n) for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); \
                                i += (int64_t)gridDim.x * blockDim.x)
 
@@ -117,13 +139,20 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPt
     P.c[p] = c;
     P.mass[p] = vol * rho;
     HN[p] = hroot<D, R>(vol);
-    R* rc = P.rec + 8 * p;
-    for (int d = 0; d < 3; d++) rc[d] = (d < D) ? x[d] : R(0);
-    rc[3] = vol;
-    rc[4] = rho;
-    rc[5] = c;
-    rc[6] = (R)ph;
-    rc[7] = R(0);
+    /* the shifting sum's record: position and volume, the phase in the
+     * volume's sign (two phases), density and sound speed apart (read only
+     * for pairs across the interface) */
+    static_assert(F == 2, "the record's sign carries one of two phases");
+    typename Vec4<R>::T r4;
+    r4.x = x[0];
+    r4.y = x[1];
+    r4.z = (D == 3) ? x[2] : R(0);
+    r4.w = copysign(vol, ph == 2 ? R(-1) : R(1));
+    reinterpret_cast<typename Vec4<R>::T*>(P.rec)[p] = r4;
+    typename Vec2<R>::T r2;
+    r2.x = rho;
+    r2.y = c;
+    reinterpret_cast<typename Vec2<R>::T*>(P.rec2)[p] = r2;
   }
   if (nfb) atomicAdd(&P.cnt->g2p_fb, nfb);
 }
@@ -189,16 +218,6 @@ __host__ __device__ constexpr bool pst_direct(int var) { return var == 2 || var 
 constexpr int PST_THREADS = 256;
 constexpr int PST_BUF = 64;
 
-template <typename R>
-struct Vec4;
-template <>
-struct Vec4<float> {
-  using T = float4;
-};
-template <>
-struct Vec4<double> {
-  using T = double4;
-};
 
 template <typename R>
 struct RowKey;
@@ -302,8 +321,9 @@ struct PstPart {
     else return dd <= lim2;
   }
 
-  /* one neighbour's contribution (particle_flow.cpp:540-575) */
-  __device__ __forceinline__ void add(const R* xnq, R volq, R rhoq, R cq, int phq, const R* nq) {
+  /* one neighbour's contribution (particle_flow.cpp:540-575); rc2 holds the
+   * neighbour's density and sound speed, read only across the interface */
+  __device__ __forceinline__ void add(const R* xnq, R volq, int phq, const R* rc2, const R* nq) {
     R dr[3];
     R d2 = R(0);
     for (int d = 0; d < D; d++) {
@@ -336,6 +356,7 @@ struct PstPart {
     if (phq != PGDG_PHASE_BOUNDARY) {
       for (int d = 0; d < D; d++) pst[d] += dr[d] * aw * tmp1 * volq;
       if (phq != ph) {
+        const R rhoq = rc2[0], cq = rc2[1];
         R tmp2 = R(1.) / (rho_p + rhoq);
         R cs = R(-0.1) * tmp2 * (crho_p + cq * cq * rhoq);
         for (int d = 0; d < D; d++) phs[d] += cs * (dr[d] * aw) * volq;
@@ -356,18 +377,27 @@ __device__ __forceinline__ void pst_boundary_cell(const CaseK& K, const DevPtrs<
       xb[d] = P.bx[d * K.nbnd + b];
       nb[d] = P.bn[d * K.nbnd + b];
     }
-    if (pp.member(xb)) pp.add(xb, (R)K.bvol, (R)K.brho, R(0), PGDG_PHASE_BOUNDARY, nb);
+    if (pp.member(xb)) pp.add(xb, (R)K.bvol, PGDG_PHASE_BOUNDARY, nullptr, nb);
   }
 }
 
-/* member record (new x, vol, rho, c, phase) written by G2P */
+/* a member's contribution from the record G2P wrote: (new x, signed volume),
+ * with density and sound speed in the second array */
+template <typename R>
+__device__ __forceinline__ int rec_phase(R w) {
+  return signbit(w) ? 2 : 1;
+}
+template <int D, typename R, bool EX>
+__device__ __forceinline__ void pst_rec_add(const DevPtrs<R>& P, int32_t q, const typename Vec4<R>::T& a,
+                                            PstPart<D, R, EX>& pp) {
+  R xnq[3] = {a.x, a.y, a.z};
+  pp.add(xnq, fabs(a.w), rec_phase(a.w), P.rec2 + 2 * (int64_t)q, nullptr);
+}
 template <int D, typename R, bool EX>
 __device__ __forceinline__ void pst_rec(const DevPtrs<R>& P, int32_t q, PstPart<D, R, EX>& pp) {
   using V4 = typename Vec4<R>::T;
-  const V4* rc = reinterpret_cast<const V4*>(P.rec + 8 * (int64_t)q);
-  const V4 a = rc[0], b = rc[1];
-  R xnq[3] = {a.x, a.y, a.z};
-  pp.add(xnq, a.w, b.x, b.y, (int)b.z, nullptr);
+  const V4 a = reinterpret_cast<const V4*>(P.rec)[q];
+  pst_rec_add<D, R, EX>(P, q, a, pp);
 }
 
 template <int D, typename R, bool EX>
@@ -682,12 +712,10 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
         /* two records in flight before either is summed (order kept) */
         const int e0 = sm->buf[i * PST_THREADS + threadIdx.x];
         const int e1 = sm->buf[(i + 1) * PST_THREADS + threadIdx.x];
-        const V4* r0 = reinterpret_cast<const V4*>(P.rec + 8 * (int64_t)slot_of<R>(sm->ent[e0].w));
-        const V4* r1 = reinterpret_cast<const V4*>(P.rec + 8 * (int64_t)slot_of<R>(sm->ent[e1].w));
-        const V4 a0 = r0[0], b0 = r0[1], a1 = r1[0], b1 = r1[1];
-        R x0[3] = {a0.x, a0.y, a0.z}, x1[3] = {a1.x, a1.y, a1.z};
-        pp.add(x0, a0.w, b0.x, b0.y, (int)b0.z, nullptr);
-        pp.add(x1, a1.w, b1.x, b1.y, (int)b1.z, nullptr);
+        const int32_t q0 = slot_of<R>(sm->ent[e0].w), q1 = slot_of<R>(sm->ent[e1].w);
+        const V4 a0 = reinterpret_cast<const V4*>(P.rec)[q0], a1 = reinterpret_cast<const V4*>(P.rec)[q1];
+        pst_rec_add<D, R, EX>(P, q0, a0, pp);
+        pst_rec_add<D, R, EX>(P, q1, a1, pp);
       }
       if (i < nbuf) {
         const int e = sm->buf[i * PST_THREADS + threadIdx.x];

@@ -91,8 +91,9 @@ struct DevPtrs {
   R *vol, *vol0, *mass, *rho, *E, *c, *P;
   R *rhov, *v, *tv; /* D*cap */
   R* sl;            /* U*D*cap: coef[0] columns 1..D */
-  R* rec;           /* 8*cap: per-particle record read by the shifting sum
-                     * (new x[3], vol, rho, c, phase, 0), written by G2P */
+  R* rec;           /* 4*cap: per-particle record of the shifting sum, written
+                     * by G2P: new x[3] and the volume signed by the phase */
+  R* rec2;          /* 2*cap: density and sound speed of the same particle */
   int8_t* phase;    /* 0 = tombstone */
   int8_t* mark_in;
   uint64_t* seq;

@@ -216,6 +216,8 @@ __host__ __device__ constexpr int pst_threads(int var) { return var == 6 ? 1024 
 __host__ __device__ constexpr int pst_minblocks(int var) { return var == 3 ? 3 : var == 6 ? 1 : 2; }
 __host__ __device__ constexpr bool pst_direct(int var) { return var == 2 || var == 3 || var == 5 || var == 6; }
 constexpr int PST_THREADS = 256;
+/* direct-sum variants test two candidates of a row per pass */
+constexpr bool PST_PAIRS = true;
 constexpr int PST_BUF = 64;
 
 
@@ -288,7 +290,7 @@ __device__ inline void pst_carve(PstSmem<D, R>& sm, unsigned char* raw, int qdep
 template <int D, typename R, bool EX>
 struct PstPart {
   R xsp[3], xnp[3];
-  R hs_p, hh, lim2, rho_p, c_p, crho_p, tmp1c, C, W_dp, inv_hh, inv_wdp, aw_c;
+  R hs_p, hh, lim2, rho_p, c_p, crho_p, tmp1c, C, W_dp, inv_hh, inv_wdp, aw_c, cwr, tmp1c5;
   int ph;
   R pst[3], phs[3];
 
@@ -308,6 +310,8 @@ struct PstPart {
     inv_hh = R(1) / hh;
     inv_wdp = R(1) / W_dp;
     aw_c = R(-5.) * C * inv_hh * inv_hh; /* dW/dr / r = -5 C q^3 / h^2 */
+    cwr = C * inv_wdp;
+    tmp1c5 = R(0.2) * tmp1c;
     for (int d = 0; d < 3; d++) pst[d] = phs[d] = R(0);
   }
 
@@ -331,8 +335,39 @@ struct PstPart {
       d2 = (d == 0) ? dr[d] * dr[d] : d2 + dr[d] * dr[d];
     }
     if (d2 == R(0)) return;
+    if constexpr (!EX) {
+      /* the same terms with the particle's constant factors folded
+       * (cwr = C / W_dp, tmp1c5 = 0.2 tmp1c) and the factor common to the
+       * components hoisted */
+      R s;
+      if constexpr (sizeof(R) == 4) s = d2 * rsqrtf(d2) * inv_hh;
+      else s = sqrt_r<R>(d2) * inv_hh;
+      if (!(s < R(2))) return; /* W and dW vanish beyond the support */
+      const R q = R(1.) - R(0.5) * s;
+      const R q2 = q * q, q3 = q2 * q;
+      const R w = (q2 * q2) * (R(1.) + R(2.) * s); /* W / C */
+      const R rr = cwr * w;                        /* W / W_dp */
+      const R rr2 = rr * rr;
+      const R tmp1 = tmp1c + tmp1c5 * (rr2 * rr2); /* tmp1c (1 + 0.2 (W / W_dp)^4) */
+      if (phq != PGDG_PHASE_BOUNDARY) {
+        const R f = aw_c * q3 * tmp1 * volq;
+        for (int d = 0; d < D; d++) pst[d] += dr[d] * f;
+        if (phq != ph) {
+          const R rhoq = rc2[0], cq = rc2[1];
+          const R tmp2 = R(1.) / (rho_p + rhoq);
+          const R cs = R(-0.1) * tmp2 * (crho_p + cq * cq * rhoq);
+          const R g = cs * aw_c * q3 * volq;
+          for (int d = 0; d < D; d++) phs[d] += dr[d] * g;
+        }
+      } else {
+        const R f = C * w * tmp1 * volq;
+        for (int d = 0; d < D; d++) pst[d] += nq[d] * f;
+      }
+      return;
+    }
+    /* exact path: the reference's operation order */
     R s, q, q3, Wij, aw, rr;
-    if constexpr (EX) {
+    {
       R dist = sqrt_r<R>(d2);
       s = dist / hh;
       if (!(s < R(2))) return; /* W and dW vanish beyond the support */
@@ -341,15 +376,6 @@ struct PstPart {
       Wij = C * (q3 * q) * (R(1.) + R(2.) * s);
       aw = R(-5.) * C * q3 * s / hh / dist;
       rr = Wij / W_dp;
-    } else {
-      if constexpr (sizeof(R) == 4) s = d2 * rsqrtf(d2) * inv_hh;
-      else s = sqrt_r<R>(d2) * inv_hh;
-      if (!(s < R(2))) return;
-      q = R(1.) - R(0.5) * s;
-      q3 = (q * q) * q;
-      Wij = C * (q3 * q) * (R(1.) + R(2.) * s);
-      aw = aw_c * q3;
-      rr = Wij * inv_wdp;
     }
     R Rr = R(0.2) * ((rr * rr) * (rr * rr));
     R tmp1 = tmp1c * (R(1) + Rr);
@@ -765,20 +791,50 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
               if (zm < za) e = m + 1;
               else hi_e = m;
             }
-            for (; e < e1; e++) {
-              const auto v = sm->ent[e];
-              const R zv = (RA == 2) ? v.z : v.y;
-              if (zv > zb) break;
-              const int ce = sm->ecell[e];
-              if (ce < clo || ce > chi) continue;
+            /* a candidate: inside the chord, in the cell window, within 2h at
+             * the stage start */
+            auto is_member = [&](const typename Vec4<R>::T& v, int ce) {
+              if ((unsigned)(ce - clo) > (unsigned)(chi - clo)) return false;
               R xsq[3] = {v.x, v.y, D == 3 ? v.z : R(0)};
-              if (pp.member(xsq)) {
-                if constexpr (pst_direct(VAR)) {
-                  pst_rec<D, R, EX>(P, slot_of<R>(v.w), pp); /* summed at once, same order */
-                } else {
-                  if (nbuf == BUFV) flush();
-                  sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)e;
+              return pp.member(xsq);
+            };
+            auto take = [&](const typename Vec4<R>::T& v, int ei) {
+              if constexpr (pst_direct(VAR)) {
+                pst_rec<D, R, EX>(P, slot_of<R>(v.w), pp); /* summed at once, same order */
+              } else {
+                if (nbuf == BUFV) flush();
+                sm->buf[nbuf++ * PST_THREADS + threadIdx.x] = (unsigned short)ei;
+              }
+            };
+            if constexpr (PST_PAIRS && pst_direct(VAR)) {
+              /* two candidates per pass (independent tests), summed in order */
+              bool more = true;
+              for (; more && e + 1 < e1; e += 2) {
+                const auto v0 = sm->ent[e], v1 = sm->ent[e + 1];
+                const R z0 = (RA == 2) ? v0.z : v0.y, z1 = (RA == 2) ? v1.z : v1.y;
+                const int c0 = sm->ecell[e], c1 = sm->ecell[e + 1];
+                if (z0 > zb) {
+                  more = false;
+                  break;
                 }
+                const bool m0 = is_member(v0, c0);
+                const bool in1 = !(z1 > zb);
+                const bool m1 = in1 && is_member(v1, c1);
+                if (m0) take(v0, e);
+                if (m1) take(v1, e + 1);
+                more = in1;
+              }
+              if (more && e < e1) {
+                const auto v = sm->ent[e];
+                const R zv = (RA == 2) ? v.z : v.y;
+                if (!(zv > zb) && is_member(v, sm->ecell[e])) take(v, e);
+              }
+            } else {
+              for (; e < e1; e++) {
+                const auto v = sm->ent[e];
+                const R zv = (RA == 2) ? v.z : v.y;
+                if (zv > zb) break;
+                if (is_member(v, sm->ecell[e])) take(v, e);
               }
             }
           }

@@ -52,7 +52,7 @@ struct pgdg_ctx {
   virtual int used_state() = 0;
   virtual int bin() = 0;
   virtual int split() = 0;
-  virtual int merge() = 0;
+  virtual int merge(bool chained = false) = 0;
   virtual int refresh_membership() = 0;
   virtual int refresh_neighbors() = 0;
   virtual int p2g() = 0;
@@ -773,8 +773,8 @@ struct Ctx : pgdg_ctx {
     timed("split", 12, [&] { Launch<D, R, EX>::split(K, P, st); });
     return PGDG_OK;
   }
-  int merge() override {
-    timed("merge", 13, [&] { Launch<D, R, EX>::merge(K, P, st); });
+  int merge(bool chained = false) override {
+    timed("merge", 14, [&] { Launch<D, R, EX>::merge(K, P, chained, st); });
     return PGDG_OK;
   }
   /* flag 4: a cell's particle list is its bucket and a particle's in_ele[0]
@@ -893,7 +893,7 @@ struct Ctx : pgdg_ctx {
     if (n == 1) used_state();
     bin();
     split();
-    for (int it = 0; it < cs.merge_iters; it++) merge();
+    for (int it = 0; it < cs.merge_iters; it++) merge(it > 0);
     refresh_membership();
     for (int md = 0; md < 2; md++) {
       refresh_neighbors();

@@ -522,8 +522,8 @@ __global__ void k_aff_cells(CaseK K, DevPtrs<R> P) {
 /* Refresh_neighbor_info(3) for affected particles: dist <= 2 p_sz within +-2 cells
  * (level_infor.cpp:161-188); stored fluid entries in list order */
 template <int D, typename R>
-__global__ void k_refresh3(CaseK K, DevPtrs<R> P) {
-  const int64_t n = (int64_t)P.cnt->n_slots;
+__global__ void k_refresh3(CaseK K, DevPtrs<R> P, const unsigned long long* np) {
+  const int64_t n = (int64_t)*np;
   const R* X = P.X[P.xb];
   const double lim = dmul(K.p_sz, 2.);
   const float lo2 = (float)(lim * lim * (1.0 - 1e-5)), hi2 = (float)(lim * lim * (1.0 + 1e-5));
@@ -651,7 +651,7 @@ void Launch<D, R, EX>::split(const CaseK& K, const DevPtrs<R>& P, cudaStream_t s
   k_split_finish<D, R><<<1, 1, 0, st>>>(K, P);
   k_bucket_fix<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P, 0);
   k_aff_cells<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P);
-  k_refresh3<D, R><<<g, BLK, 0, st>>>(K, P);
+  k_refresh3<D, R><<<g, BLK, 0, st>>>(K, P, &P.cnt->n_slots);
   k_mark_in<D, R><<<g, BLK, 0, st>>>(K, P, nullptr);
   k_reset_queues<R><<<1, 1, 0, st>>>(P);
 }
@@ -659,9 +659,18 @@ void Launch<D, R, EX>::split(const CaseK& K, const DevPtrs<R>& P, cudaStream_t s
 /* ------------------------------------------------------------------ */
 /* merge (one pass of Merge_particle_fast)                            */
 /* ------------------------------------------------------------------ */
+/* particles a merge pass sweeps: all slots, or none when the pass follows a
+ * pass of the same sequence that merged nothing (the state is then unchanged,
+ * so this pass would recompute the same partners and merge nothing too) */
+template <typename R>
+__global__ void k_merge_begin(DevPtrs<R> P, int chained) {
+  DevCounters* c = P.cnt;
+  c->merge_n = (chained && c->merge_quiet) ? 0ull : c->n_slots;
+}
+
 template <int D, typename R>
 __global__ void k_merge_a(CaseK K, DevPtrs<R> P) {
-  const int64_t n = (int64_t)P.cnt->n_slots;
+  const int64_t n = (int64_t)P.cnt->merge_n;
   const R* X = P.X[P.xb];
   GRID_STRIDE(p, n) {
     P.target[p] = -1;
@@ -699,7 +708,7 @@ __global__ void k_merge_a(CaseK K, DevPtrs<R> P) {
 
 template <int D, typename R>
 __global__ void k_merge_b(CaseK K, DevPtrs<R> P) {
-  const int64_t n = (int64_t)P.cnt->n_slots;
+  const int64_t n = (int64_t)P.cnt->merge_n;
   GRID_STRIDE(p, n) {
     unsigned long long s = 0;
     int32_t q = P.target[p];
@@ -716,7 +725,7 @@ __global__ void k_merge_b(CaseK K, DevPtrs<R> P) {
 template <int D, typename R>
 __global__ void k_merge_c(CaseK K, DevPtrs<R> P) {
   constexpr int NS = PState<D>::NS;
-  const int64_t n = (int64_t)P.cnt->n_slots;
+  const int64_t n = (int64_t)P.cnt->merge_n;
   const unsigned long long app = P.cnt->append_next;
   GRID_STRIDE(p, n) {
     if (P.mflag[p] != 1) continue;
@@ -756,7 +765,7 @@ __global__ void k_merge_c(CaseK K, DevPtrs<R> P) {
 
 template <typename R>
 __global__ void k_aff_oldnbr_merge(CaseK K, DevPtrs<R> P) {
-  const int64_t n = (int64_t)P.cnt->n_slots;
+  const int64_t n = (int64_t)P.cnt->merge_n;
   GRID_STRIDE(p, n) {
     if (P.mflag[p] != 1) continue;
     int32_t q = P.target[p];
@@ -785,20 +794,22 @@ __global__ void k_merge_finish(CaseK K, DevPtrs<R> P) {
   c->append_next += ns;
   c->n_live -= ns;
   c->n_merge += ns;
+  c->merge_quiet = ns == 0 ? 1ull : 0ull;
 }
 
 template <int D, typename R, bool EX>
-void Launch<D, R, EX>::merge(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
+void Launch<D, R, EX>::merge(const CaseK& K, const DevPtrs<R>& P, bool chained, cudaStream_t st) {
   const int g = grid_for(K.cap, BLK);
+  k_merge_begin<R><<<1, 1, 0, st>>>(P, chained ? 1 : 0);
   k_merge_a<D, R><<<g, BLK, 0, st>>>(K, P);
   k_merge_b<D, R><<<g, BLK, 0, st>>>(K, P);
-  scan_u64(P.scan, P.scan_blk, &P.cnt->n_slots, K.cap, st);
+  scan_u64(P.scan, P.scan_blk, &P.cnt->merge_n, K.cap, st);
   k_aff_oldnbr_merge<R><<<g, BLK, 0, st>>>(K, P);
   k_merge_c<D, R><<<g, BLK, 0, st>>>(K, P);
   k_merge_finish<D, R><<<1, 1, 0, st>>>(K, P);
   k_bucket_fix<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P, 0);
   k_aff_cells<R><<<grid_for(P.qcap, BLK), BLK, 0, st>>>(K, P);
-  k_refresh3<D, R><<<g, BLK, 0, st>>>(K, P);
+  k_refresh3<D, R><<<g, BLK, 0, st>>>(K, P, &P.cnt->merge_n);
   /* the pass's merge count is still the scan total */
   k_mark_in<D, R><<<g, BLK, 0, st>>>(K, P, P.scan_blk + scan_nblk(K.cap));
   k_reset_queues<R><<<1, 1, 0, st>>>(P);
@@ -910,7 +921,7 @@ void Launch<D, R, EX>::reset_lists(const CaseK& K, const DevPtrs<R>& P, cudaStre
 #define PGDG_INST(D, R, EX)                                                          \
   template void Launch<D, R, EX>::bin(const CaseK&, const DevPtrs<R>&, cudaStream_t);  \
   template void Launch<D, R, EX>::split(const CaseK&, const DevPtrs<R>&, cudaStream_t); \
-  template void Launch<D, R, EX>::merge(const CaseK&, const DevPtrs<R>&, cudaStream_t); \
+  template void Launch<D, R, EX>::merge(const CaseK&, const DevPtrs<R>&, bool, cudaStream_t); \
   template void Launch<D, R, EX>::store_lists(const CaseK&, const DevPtrs<R>&, int, int, int, cudaStream_t); \
   template void Launch<D, R, EX>::reset_lists(const CaseK&, const DevPtrs<R>&, cudaStream_t);
 PGDG_INST(2, double, false)

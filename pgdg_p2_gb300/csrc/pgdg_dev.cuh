@@ -50,6 +50,8 @@ struct DevCounters {
   unsigned long long mgfm_calls, mgfm_iters, mgfm_maxit, g2p_fb;
   unsigned long long dt_bits, maxv_bits; /* atomic min/max scratch */
   unsigned long long queue_n;
+  unsigned long long merge_n;     /* slots the current merge pass sweeps */
+  unsigned long long merge_quiet; /* the last merge pass merged nothing */
   unsigned int err;
   unsigned int pad;
   double dt, max_v;
@@ -194,7 +196,9 @@ struct Launch {
   /* k_particles.cu */
   static void bin(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void split(const CaseK&, const DevPtrs<R>&, cudaStream_t);
-  static void merge(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  /* chained: the pass follows another of the same sequence (it is skipped
+   * on the device when that one merged nothing) */
+  static void merge(const CaseK&, const DevPtrs<R>&, bool chained, cudaStream_t);
   static void store_lists(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, cudaStream_t);
   static void reset_lists(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   /* k_grid.cu */

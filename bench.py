@@ -328,14 +328,15 @@ def run_ours(args):
                      "p2g": ncell * (2 * 4 + 2 * 20 * 4) + N * (3 * 4 + 4 + 1),
                      "limiter": ncell * (2 * 20 * 4 * 1 + 2 * 9 * 4 * 2 + 2 * 5 * 4 + 9 * 4)}.get(dom, 0)
         achieved = bytes_per / (per_launch_ms / 1e3) / 1e9
-        # FP32 work of the shifting kernel: ~137 pairs x 50 flop per particle (3D, 8 ppc)
-        flops_per = {"pst": N * 137 * 50, "grid_acc": ncell * 13000}.get(dom, 0)
+        # FP32 work of the shifting kernel per particle (3D lattice, 8 per cell): 228
+        # candidates x 8 flop (distance test) + 147 members x 33 flop (pair term)
+        flops_per = {"pst": N * (228 * 8 + 147 * 33), "grid_acc": ncell * 13000}.get(dom, 0)
         sm_mhz = peaks.get("sm_max_mhz", 2070.0)
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         # DRAM traffic per shifting launch from the ncu capture of the 192x48x48 case
-        # (433.6 MB read + written for 3,538,944 particles), scaled by the particle
+        # (429.4 MB read + written for 3,538,944 particles), scaled by the particle
         # count (the traffic grows with it)
-        traffic = 433.6e6 * N / 3538944 if dom == "pst" and CONFIG_ID == 3 else None
+        traffic = 429.4e6 * N / 3538944 if dom == "pst" and CONFIG_ID == 3 else None
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "traffic_note": "bytes per launch, ncu capture of "
                 "the 192x48x48 case scaled by particles" if traffic else None,

@@ -880,10 +880,11 @@ struct Ctx : pgdg_ctx {
       if (xn == xs || xn == x0 || xn < 0 || xn > 2) xn = (xs + 1) % 3;  /* md 1 without md 0 */
     }
     timed("g2p", 1, [&] { Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, st); });
+    if (!EX) timed("rowsort", 3, [&] { Launch<D, R, EX>::rowsort(K, P, xs, pst_scratch, st); });
     if (pst_var < 0)
       pst_var = tune(Launch<D, R, EX>::pst_variants(),
                      [&](int v) { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, v, pst_scratch, st); });
-    timed("pst", EX ? 1 : 4, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, pst_var, pst_scratch, st); });
+    timed("pst", 1, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, pst_var, pst_scratch, st); });
     if (md == 1) timed("store_lists", 2, [&] { Launch<D, R, EX>::store_lists(K, P, xs, hs, xn, st); });
     P.xb = xn;
     P.hb = hn;

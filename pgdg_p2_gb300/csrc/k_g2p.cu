@@ -1251,8 +1251,22 @@ size_t Launch<D, R, EX>::pst_scratch_bytes(const CaseK& K) {
   return EX ? 0 : rowsort_layout<R>(K, nullptr, nullptr);
 }
 
-/* launches: the exact path 1; otherwise the three row-sort passes and the
- * shifting kernel (4) */
+/* the per-stage row sort of the mixed and FMA paths (three launches; nothing
+ * on the exact path) */
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::rowsort(const CaseK& K, const DevPtrs<R>& P, int xs, void* scratch, cudaStream_t st) {
+  if constexpr (!EX) {
+    RowSortBufs<R> B;
+    rowsort_layout<R>(K, static_cast<unsigned char*>(scratch), &B);
+    const int64_t nrows = K.ncell / K.N[D - 1];
+    k_rs_cells<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, xs, B);
+    k_rs_rows<D, R><<<grid_for(nrows, 128), 128, 0, st>>>(K, P, B);
+    k_rs_rank<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, B);
+  }
+}
+
+/* the shifting kernel (one launch); on the mixed and FMA paths it reads the
+ * rows sorted by rowsort() for the same stage */
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, int var,
                            void* scratch, cudaStream_t st) {
@@ -1261,10 +1275,6 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
   } else {
     RowSortBufs<R> B;
     rowsort_layout<R>(K, static_cast<unsigned char*>(scratch), &B);
-    const int64_t nrows = K.ncell / K.N[D - 1];
-    k_rs_cells<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, xs, B);
-    k_rs_rows<D, R><<<grid_for(nrows, 128), 128, 0, st>>>(K, P, B);
-    k_rs_rank<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, B);
     const RowSorted<R> RS{B.row, B.rk, B.pmin, B.pmax};
     if (var == 1) pst_launch<D, R, EX, 1>(K, P, xs, hs, xn, hn, RS, st);
     else if (var == 2) pst_launch<D, R, EX, 2>(K, P, xs, hs, xn, hn, RS, st);
@@ -1280,6 +1290,7 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
   template void Launch<D, R, EX>::pst(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, void*,        \
                                       cudaStream_t);                                                       \
   template size_t Launch<D, R, EX>::pst_scratch_bytes(const CaseK&);                                       \
+  template void Launch<D, R, EX>::rowsort(const CaseK&, const DevPtrs<R>&, int, void*, cudaStream_t);        \
   template int Launch<D, R, EX>::pst_variants();
 #ifdef PGDG_EXACT_TU
 PGDG_INST(2, double, true)

@@ -220,6 +220,9 @@ struct Launch {
   static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, int var, void* scratch,
                   cudaStream_t);
   static size_t pst_scratch_bytes(const CaseK&);
+  /* per-stage row sort the shifting kernel of the same stage reads (mixed and
+   * FMA paths; no launch on the exact path) */
+  static void rowsort(const CaseK&, const DevPtrs<R>&, int xs, void* scratch, cudaStream_t);
   static int pst_variants();
 };
 

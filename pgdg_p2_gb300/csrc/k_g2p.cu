@@ -553,59 +553,137 @@ __host__ __device__ inline size_t rowsort_layout(const CaseK& K, unsigned char* 
   return o;
 }
 
+/* k_rs_cells sorts a cell's run in shared memory when it holds at most
+ * RS_CAP entries (entry i of thread t at [i][t], so that a warp's accesses fall
+ * on consecutive banks); a fuller cell sorts in place in global memory */
+constexpr int RS_T = 128, RS_CAP = 16;
+
 template <int D, typename R>
-__global__ void __launch_bounds__(256) k_rs_cells(CaseK K, DevPtrs<R> P, int xs, RowSortBufs<R> B) {
+__global__ void __launch_bounds__(RS_T) k_rs_cells(CaseK K, DevPtrs<R> P, int xs, RowSortBufs<R> B) {
   using V4 = typename Vec4<R>::T;
+  extern __shared__ __align__(32) unsigned char rs_raw[];
+  V4* sh = reinterpret_cast<V4*>(rs_raw);
   const R* XS = P.X[xs];
+  const int t = threadIdx.x;
   GRID_STRIDE(c, K.ncell) {
     const int cnt = min(P.bcnt[c], K.maxpc);
     const int64_t base = c * K.maxpc;
-    for (int r = 0; r < cnt; r++) {
+    auto load = [&](int r) {
       const int32_t q = P.bucket[base + r];
       V4 v;
       v.x = XS[q];
       v.y = XS[K.cap + q];
       v.z = (D == 3) ? XS[2 * K.cap + q] : R(0);
       v.w = slot_as<R>(q);
-      const RowKey<R> key = RowKey<R>::of(v, D - 1);
-      int j = r - 1;
-      while (j >= 0) {
-        const V4 u = B.run[base + j];
-        if (RowKey<R>::of(u, D - 1).lt(key)) break;
-        B.run[base + j + 1] = u;
-        j--;
+      return v;
+    };
+    if (cnt <= RS_CAP) {
+      for (int r = 0; r < cnt; r++) {
+        const V4 v = load(r);
+        const RowKey<R> key = RowKey<R>::of(v, D - 1);
+        int j = r - 1;
+        while (j >= 0) {
+          const V4 u = sh[j * RS_T + t];
+          if (RowKey<R>::of(u, D - 1).lt(key)) break;
+          sh[(j + 1) * RS_T + t] = u;
+          j--;
+        }
+        sh[(j + 1) * RS_T + t] = v;
       }
-      B.run[base + j + 1] = v;
+      for (int r = 0; r < cnt; r++) B.run[base + r] = sh[r * RS_T + t];
+      B.kmin[c] = cnt ? RowKey<R>::of(sh[t], D - 1) : RowKey<R>::highest();
+      B.kmax[c] = cnt ? RowKey<R>::of(sh[(cnt - 1) * RS_T + t], D - 1) : RowKey<R>::lowest();
+    } else {
+      for (int r = 0; r < cnt; r++) {
+        const V4 v = load(r);
+        const RowKey<R> key = RowKey<R>::of(v, D - 1);
+        int j = r - 1;
+        while (j >= 0) {
+          const V4 u = B.run[base + j];
+          if (RowKey<R>::of(u, D - 1).lt(key)) break;
+          B.run[base + j + 1] = u;
+          j--;
+        }
+        B.run[base + j + 1] = v;
+      }
+      B.kmin[c] = RowKey<R>::of(B.run[base], D - 1);
+      B.kmax[c] = RowKey<R>::of(B.run[base + cnt - 1], D - 1);
     }
-    B.kmin[c] = cnt ? RowKey<R>::of(B.run[base], D - 1) : RowKey<R>::highest();
-    B.kmax[c] = cnt ? RowKey<R>::of(B.run[base + cnt - 1], D - 1) : RowKey<R>::lowest();
   }
 }
 
+/* warp shuffles of a row key */
+__device__ __forceinline__ RowKey<float> rk_shfl(const RowKey<float>& a, int src) {
+  return RowKey<float>{__shfl_sync(0xffffffffu, a.k, src)};
+}
+__device__ __forceinline__ RowKey<double> rk_shfl(const RowKey<double>& a, int src) {
+  return RowKey<double>{__shfl_sync(0xffffffffu, a.z, src), __shfl_sync(0xffffffffu, a.s, src)};
+}
+__device__ __forceinline__ RowKey<float> rk_shfl_up(const RowKey<float>& a, int o) {
+  return RowKey<float>{__shfl_up_sync(0xffffffffu, a.k, o)};
+}
+__device__ __forceinline__ RowKey<double> rk_shfl_up(const RowKey<double>& a, int o) {
+  return RowKey<double>{__shfl_up_sync(0xffffffffu, a.z, o), __shfl_up_sync(0xffffffffu, a.s, o)};
+}
+__device__ __forceinline__ RowKey<float> rk_shfl_down(const RowKey<float>& a, int o) {
+  return RowKey<float>{__shfl_down_sync(0xffffffffu, a.k, o)};
+}
+__device__ __forceinline__ RowKey<double> rk_shfl_down(const RowKey<double>& a, int o) {
+  return RowKey<double>{__shfl_down_sync(0xffffffffu, a.z, o), __shfl_down_sync(0xffffffffu, a.s, o)};
+}
+
+/* one warp per row: run offsets (a running sum), prefix maxima of the runs'
+ * largest keys and suffix minima of their smallest keys, 32 cells at a time */
 template <int D, typename R>
 __global__ void __launch_bounds__(128) k_rs_rows(CaseK K, DevPtrs<R> P, RowSortBufs<R> B) {
   const int NR = K.N[D - 1];
   const int64_t nrows = K.ncell / NR;
-  GRID_STRIDE(rw, nrows) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t rw = w0; rw < nrows; rw += nw) {
     const int64_t c0 = rw * NR;
-    int acc = 0;
-    RowKey<R> mx = RowKey<R>::lowest();
-    for (int k = 0; k < NR; k++) {
+    int carry = 0;
+    RowKey<R> mxc = RowKey<R>::lowest();
+    for (int k0 = 0; k0 < NR; k0 += 32) {
+      const int k = k0 + lane;
+      const bool valid = k < NR;
       const int64_t c = c0 + k;
-      B.off[c] = acc;
-      acc += min(P.bcnt[c], K.maxpc);
-      const RowKey<R> km = B.kmax[c];
-      if (mx.lt(km)) mx = km;
-      B.pmaxk[c] = mx;
-      B.pmin[c] = INT_MAX;
-      B.pmax[c] = -1;
+      const int cnt = valid ? min(P.bcnt[c], K.maxpc) : 0;
+      int inc = cnt;
+      RowKey<R> m = valid ? B.kmax[c] : RowKey<R>::lowest();
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        const RowKey<R> z = rk_shfl_up(m, o);
+        if (lane >= o) {
+          inc += y;
+          if (m.lt(z)) m = z;
+        }
+      }
+      if (valid) {
+        B.off[c] = carry + inc - cnt;
+        B.pmaxk[c] = mxc.lt(m) ? m : mxc;
+        B.pmin[c] = INT_MAX;
+        B.pmax[c] = -1;
+      }
+      carry += __shfl_sync(0xffffffffu, inc, 31);
+      const RowKey<R> top = rk_shfl(m, 31);
+      if (mxc.lt(top)) mxc = top;
     }
-    RowKey<R> mn = RowKey<R>::highest();
-    for (int k = NR - 1; k >= 0; k--) {
-      const int64_t c = c0 + k;
-      const RowKey<R> km = B.kmin[c];
-      if (km.lt(mn)) mn = km;
-      B.smink[c] = mn;
+    RowKey<R> mnc = RowKey<R>::highest();
+    for (int k0 = ((NR - 1) / 32) * 32; k0 >= 0; k0 -= 32) {
+      const int k = k0 + lane;
+      const bool valid = k < NR;
+      RowKey<R> m = valid ? B.kmin[c0 + k] : RowKey<R>::highest();
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const RowKey<R> z = rk_shfl_down(m, o);
+        if (lane + o < 32 && z.lt(m)) m = z;
+      }
+      if (valid) B.smink[c0 + k] = m.lt(mnc) ? m : mnc;
+      const RowKey<R> bot = rk_shfl(m, 0);
+      if (bot.lt(mnc)) mnc = bot;
     }
   }
 }
@@ -1259,8 +1337,14 @@ void Launch<D, R, EX>::rowsort(const CaseK& K, const DevPtrs<R>& P, int xs, void
     RowSortBufs<R> B;
     rowsort_layout<R>(K, static_cast<unsigned char*>(scratch), &B);
     const int64_t nrows = K.ncell / K.N[D - 1];
-    k_rs_cells<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, xs, B);
-    k_rs_rows<D, R><<<grid_for(nrows, 128), 128, 0, st>>>(K, P, B);
+    const size_t shb = sizeof(typename Vec4<R>::T) * RS_CAP * RS_T;
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_rs_cells<D, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shb);
+      attr_set = true;
+    }
+    k_rs_cells<D, R><<<grid_for(K.ncell, RS_T), RS_T, shb, st>>>(K, P, xs, B);
+    k_rs_rows<D, R><<<grid_for(nrows * 32, 128), 128, 0, st>>>(K, P, B);
     k_rs_rank<D, R><<<grid_for(K.ncell, 256), 256, 0, st>>>(K, P, B);
   }
 }

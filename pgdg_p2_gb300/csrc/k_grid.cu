@@ -751,6 +751,25 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
         double xn[3] = {0, 0, 0};
         if constexpr (EX)
           if (nb >= 0) center<D>(K, fc.nb, xn);
+        /* the FP32 path takes, on an interior face, the neighbour phases as the
+         * outer loop and the quadrature points as the inner one, so that a
+         * neighbour phase's coefficients are loaded once per face; the FP64
+         * paths keep the reference's order (points outer, phases inner) */
+        constexpr bool HOIST = !EX && sizeof(R) == 4;
+        const int nso = (HOIST && fbound == 0) ? F : 1;
+        for (int so = 0; so < nso; so++) {
+        R ajo = R(0), cn[U][B], ln[U];
+        if constexpr (HOIST) {
+          if (fbound == 0) {
+            ajo = P.calph[so * nc + nb];
+            if (ajo == R(0)) continue;
+            if (MODE == 2 && so == ss) continue;
+            for (int u = 0; u < U; u++) {
+              for (int b = 0; b < B; b++) cn[u][b] = P.ccoef[((so * U + u) * B + b) * nc + nb];
+              ln[u] = P.clim[(so * U + u) * nc + nb];
+            }
+          }
+        }
         for (int qd = 0; qd < NQ; qd++) {
           int g1 = (D == 3) ? (qd >> 1) : qd, g2 = qd & 1;
           double dpv[3];
@@ -782,8 +801,8 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
           Nb[0] = R(1.);
           for (int d = 0; d < D; d++) Nb[1 + d] = dri[d];
           if (fbound == 0) {
-            for (int s1 = 0; s1 < F; s1++) {
-              const R aj = P.calph[s1 * nc + nb];
+            for (int s1 = HOIST ? so : 0; s1 < (HOIST ? so + 1 : F); s1++) {
+              const R aj = HOIST ? ajo : P.calph[s1 * nc + nb];
               if (aj == R(0)) continue;
               if (MODE == 2 && s1 == ss) continue;
               R drj[3];
@@ -794,10 +813,18 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
                 for (int d = 0; d < D; d++) drj[d] = dri[d] - R(2) * fr.cen[d];
               }
               R Uj[U];
-              for (int u = 0; u < U; u++) {
-                R acc = P.ccoef[((s1 * U + u) * B + 1) * nc + nb] * drj[0];
-                for (int b = 1; b < D; b++) acc = acc + P.ccoef[((s1 * U + u) * B + 1 + b) * nc + nb] * drj[b];
-                Uj[u] = P.ccoef[((s1 * U + u) * B) * nc + nb] + P.clim[(s1 * U + u) * nc + nb] * acc;
+              if constexpr (!HOIST) {
+                for (int u = 0; u < U; u++) {
+                  R acc = P.ccoef[((s1 * U + u) * B + 1) * nc + nb] * drj[0];
+                  for (int b = 1; b < D; b++) acc = acc + P.ccoef[((s1 * U + u) * B + 1 + b) * nc + nb] * drj[b];
+                  Uj[u] = P.ccoef[((s1 * U + u) * B) * nc + nb] + P.clim[(s1 * U + u) * nc + nb] * acc;
+                }
+              } else {
+                for (int u = 0; u < U; u++) {
+                  R acc = cn[u][1] * drj[0];
+                  for (int b = 1; b < D; b++) acc = acc + cn[u][1 + b] * drj[b];
+                  Uj[u] = cn[u][0] + ln[u] * acc;
+                }
               }
               R rho_j = Uj[0], E_j = Uj[U - 1];
               R v_j[3], rhov_j[3];
@@ -947,6 +974,7 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
             for (int b = 0; b < B; b++)
               for (int u = 0; u < U; u++) DFn[b][u] += Fh[u] * Nb[b] * gw;
           }
+        }
         }
         const R Sj = EX ? (R)fc.S : fr.S;
         for (int b = 0; b < B; b++)

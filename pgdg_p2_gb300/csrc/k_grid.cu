@@ -552,58 +552,52 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(6)) k_limiter(CaseK K, D
         u_max[s][u] = amax1(u_max[s][u], R(0.));
         u_min[s][u] = amin1(u_min[s][u], R(0.));
       }
-    for (int f = 0; f < NF; f++) {
-      R dr[3];
-      int fbound;
-      if constexpr (EX) {
-        FaceK fc;
-        face<D>(K, idx, xc, f, fc);
-        fbound = fc.bound;
-        if (fc.bound == 0) {
-          double xn[3];
-          center<D>(K, fc.nb, xn);
-          for (int d = 0; d < D; d++) dr[d] = (R)(xn[d] - xc[d]);
+    /* per phase: its coefficients are loaded once; the face limits (a minimum
+     * over the faces, so the face order does not matter) and the positivity
+     * probe (mpm.cpp:690-728) then read them from registers */
+    const int NPR = (D == 3) ? 8 : 4;
+#pragma unroll
+    for (int s = 0; s < F; s++) {
+      R co[U][B];
+      for (int u = 0; u < U; u++)
+        for (int b = 0; b < B; b++) co[u][b] = P.ccoef[((s * U + u) * B + b) * nc + ci];
+      const int lim_fg = (bd_fg || P.calph[s * nc + ci] != R(1)) ? 1 : 0;
+      for (int f = 0; f < NF; f++) {
+        R dr[3];
+        if constexpr (EX) {
+          FaceK fc;
+          face<D>(K, idx, xc, f, fc);
+          if (fc.bound == 0) {
+            double xn[3];
+            center<D>(K, fc.nb, xn);
+            for (int d = 0; d < D; d++) dr[d] = (R)(xn[d] - xc[d]);
+          } else {
+            for (int d = 0; d < D; d++) dr[d] = (R)(fc.cen[d] - xc[d]);
+          }
         } else {
-          for (int d = 0; d < D; d++) dr[d] = (R)(fc.cen[d] - xc[d]);
+          FaceRel<R> fc;
+          face_rel<D, R>(K, idx, hps, Sax, f, fc);
+          /* neighbour centre (interior) or face centre (boundary) from the cell centre */
+          for (int d = 0; d < D; d++) dr[d] = (fc.bound == 0) ? R(2) * fc.cen[d] : fc.cen[d];
         }
-      } else {
-        FaceRel<R> fc;
-        face_rel<D, R>(K, idx, hps, Sax, f, fc);
-        fbound = fc.bound;
-        /* neighbour centre (interior) or face centre (boundary) from the cell centre */
-        for (int d = 0; d < D; d++) dr[d] = (fc.bound == 0) ? R(2) * fc.cen[d] : fc.cen[d];
-      }
-      (void)fbound;
-      for (int s = 0; s < F; s++) {
-        int lim_fg = bd_fg;
-        if (P.calph[s * nc + ci] != R(1)) lim_fg = 1;
         for (int u = 0; u < U; u++) {
           R dU = R(0);
-          for (int b = 0; b < D; b++) {
-            R cf = P.ccoef[((s * U + u) * B + 1 + b) * nc + ci];
-            dU = (b == 0) ? cf * dr[b] : dU + cf * dr[b];
-          }
+          for (int b = 0; b < D; b++) dU = (b == 0) ? co[u][1 + b] * dr[b] : dU + co[u][1 + b] * dr[b];
           R sd = R(1);
           if (dU >= R(0)) sd = limiter_fn<R>(fabs(u_max[s][u] / (dU + R(1e-20))), lim_fg);
           else if (dU < R(0)) sd = limiter_fn<R>(fabs(u_min[s][u] / (dU + R(1e-20))), lim_fg);
           lim[s][u] = amin1(lim[s][u], sd);
         }
       }
-    }
-    /* positivity probe (mpm.cpp:690-728) */
-    const int NPR = (D == 3) ? 8 : 4;
-    for (int s = 0; s < F; s++) {
       const R gs = (R)K.gamma[s], pf = (R)K.pinf[s], pfe = (R)K.pinf_eos[s];
       int fg = 0;
       for (int pr = 0; pr < NPR && !fg; pr++) {
         R Ui[U];
         for (int u = 0; u < U; u++) {
           R acc = R(0);
-          for (int b = 0; b < D; b++) {
-            R cf = P.ccoef[((s * U + u) * B + 1 + b) * nc + ci];
-            acc = (b == 0) ? cf * s_probe[pr][b] : acc + cf * s_probe[pr][b];
-          }
-          Ui[u] = P.ccoef[((s * U + u) * B) * nc + ci] + lim[s][u] * acc;
+          for (int b = 0; b < D; b++)
+            acc = (b == 0) ? co[u][1 + b] * s_probe[pr][b] : acc + co[u][1 + b] * s_probe[pr][b];
+          Ui[u] = co[u][0] + lim[s][u] * acc;
         }
         R sq = Ui[1] * Ui[1];
         for (int k = 1; k < D; k++) sq = sq + Ui[1 + k] * Ui[1 + k];

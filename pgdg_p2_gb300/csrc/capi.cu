@@ -147,6 +147,9 @@ struct Ctx : pgdg_ctx {
   IfaceQ Q{};
   PartScratch part;   /* root partition of the interface batch */
   unsigned char* pst_scratch = nullptr; /* per-stage row sort of the shifting kernel */
+  /* every particle lies in its bucket's cell (true from binning until the
+   * particles move); P2G then skips neighbour cells beyond its cut radius */
+  bool fresh_bins = false;
   double *d_gam = nullptr, *d_pinf = nullptr;
   unsigned long long* d_ncell = nullptr;
 
@@ -398,6 +401,7 @@ struct Ctx : pgdg_ctx {
   /* ---------------- exchange ---------------- */
   int upload_particles(const pgdg_particles* pp) override {
     drop_graphs();
+    fresh_bins = false;
     int64_t n = pp->n;
     if (n > K.cap) {
       err = "particle count exceeds capacity";
@@ -767,6 +771,7 @@ struct Ctx : pgdg_ctx {
   }
   int bin() override {
     timed("bin", 2, [&] { Launch<D, R, EX>::bin(K, P, st); });
+    fresh_bins = true;
     return PGDG_OK;
   }
   int split() override {
@@ -784,7 +789,8 @@ struct Ctx : pgdg_ctx {
    * the shifting kernel; nothing to do here */
   int refresh_neighbors() override { return PGDG_OK; }
   int p2g() override {
-    timed("p2g", 2, [&] { Launch<D, R, EX>::p2g(K, P, st); });
+    timed("p2g", 1, [&] { Launch<D, R, EX>::p2g(K, P, fresh_bins, st); });
+    timed("p2g_new", 1, [&] { Launch<D, R, EX>::p2g_new(K, P, st); });
     return PGDG_OK;
   }
   int limiter() override {
@@ -868,6 +874,7 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
   int update_particle(int md) override {
+    fresh_bins = false;
     const int xs = P.xb, hs = P.hb, hn = 1 - P.hb;
     int x0, xn;
     if (md == 0) {

@@ -230,7 +230,7 @@ __device__ __forceinline__ R kernel_w_r(R dist, R h, R C) {
  * index, offset from the cell centre and kernel weight times volume */
 template <int D, typename R, typename F_>
 __device__ __forceinline__ void p2g_scan(const CaseK& K, const DevPtrs<R>& P, const int* idx, const double* xc,
-                                         const R* xcr, double Cw, F_&& body) {
+                                         const R* xcr, double Cw, int skip, F_&& body) {
   const R* X = P.X[P.xb];
   const double hi = K.p_g * 1 * 3.2 / CUT_OFF;
   const double cut = 1.5 * K.p_sz;
@@ -240,9 +240,13 @@ __device__ __forceinline__ void p2g_scan(const CaseK& K, const DevPtrs<R>& P, co
     lo[d] = max(idx[d] - 1, 0);
     hi3[d] = min(idx[d] + 1, (d < D ? K.N[d] : 1) - 1);
   }
+  /* skip: bit (ox | oy << 1 | oz << 2), o = offset along the axis is nonzero,
+   * set for the neighbour cells that hold no contributing particle (p2g_skip) */
   for (int t = lo[0]; t <= hi3[0]; t++)
     for (int s = lo[1]; s <= hi3[1]; s++)
       for (int m = lo[2]; m <= hi3[2]; m++) {
+        const int code = (t != idx[0] ? 1 : 0) | (s != idx[1] ? 2 : 0) | (m != idx[2] ? 4 : 0);
+        if ((skip >> code) & 1) continue;
         int64_t cn = cidx3(K, t, s, m);
         int cntq = min(P.bcnt[cn], K.maxpc);
         const int32_t* bk = P.bucket + cn * K.maxpc;
@@ -284,12 +288,36 @@ __device__ __forceinline__ void p2g_scan(const CaseK& K, const DevPtrs<R>& P, co
       }
 }
 
+/* Neighbour cells P2G can skip when every particle lies in its bucket's cell
+ * (right after binning; split children, inlet clones and merged particles are
+ * appended to the cell of their exact position): a cell whose box, shrunk by
+ * 1e-4 of a cell against rounding, stays beyond the cut radius of the centre
+ * holds no particle inside it.  Bit (ox | oy << 1 | oz << 2) for the offset
+ * pattern (o = nonzero offset along that axis).  Skipping them leaves the
+ * order of the remaining sum unchanged. */
+template <int D>
+int p2g_skip(const CaseK& K) {
+  const double cut = 1.5 * K.p_sz;
+  int mask = 0;
+  for (int code = 0; code < 8; code++) {
+    if (D == 2 && (code & 4)) continue;
+    double g2 = 0.0;
+    for (int d = 0; d < D; d++)
+      if (code & (1 << d)) {
+        const double g = 0.5 * K.ps[d] * (1.0 - 1e-4);
+        g2 += g * g;
+      }
+    if (g2 > cut * cut) mask |= 1 << code;
+  }
+  return mask;
+}
+
 /* per cell: the kernel-weighted mass of each phase in the neighbourhood, the
  * phase flags and volume fractions, and the reset of absent phases; the rare
  * newly present phases are flagged in cnew for k_p2g_new (a second kernel, so
  * that this one keeps a small register footprint) */
 template <int D, typename R, bool EX>
-__global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
+__global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw, int skip) {
   constexpr int U = D + 2, B = D + 1;
   const int64_t nc = K.ncell;
   GRID_STRIDE(ci, nc) {
@@ -304,7 +332,7 @@ __global__ void __launch_bounds__(128) k_p2g(CaseK K, DevPtrs<R> P, double Cw) {
     R xcr[3];
     for (int d = 0; d < 3; d++) xcr[d] = (R)xc[d];
     double mass_t[F] = {0, 0};
-    p2g_scan<D, R>(K, P, idx, xc, xcr, Cw, [&](int32_t, int ph, const R*, R ww) {
+    p2g_scan<D, R>(K, P, idx, xc, xcr, Cw, skip, [&](int32_t, int ph, const R*, R ww) {
 #pragma unroll
       for (int s = 0; s < F; s++)
         if (s == ph) mass_t[s] += (double)ww;
@@ -359,7 +387,7 @@ __global__ void __launch_bounds__(128) k_p2g_new(CaseK K, DevPtrs<R> P, double C
       double p_avg[U], Cf[NS], mt = 0;
       for (int u = 0; u < U; u++) p_avg[u] = 0;
       for (int t = 0; t < NS; t++) Cf[t] = 0;
-      p2g_scan<D, R>(K, P, idx, xc, xcr, Cw, [&](int32_t q, int ph, const R* xij, R ww) {
+      p2g_scan<D, R>(K, P, idx, xc, xcr, Cw, 0, [&](int32_t q, int ph, const R* xij, R ww) {
         if (ph != ss) return;
         mt += (double)ww;
         double wwd = (double)ww;
@@ -408,11 +436,19 @@ __global__ void __launch_bounds__(128) k_p2g_new(CaseK K, DevPtrs<R> P, double C
 }
 
 template <int D, typename R, bool EX>
-void Launch<D, R, EX>::p2g(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
+void Launch<D, R, EX>::p2g(const CaseK& K, const DevPtrs<R>& P, bool fresh_bins, cudaStream_t st) {
   const double hi = K.p_g * 1 * 3.2 / CUT_OFF;
   double hh = (D == 2) ? hi * hi : hi * hi * hi;
   double Cw = (D == 2) ? 1.0 / PI_REF / hh * 7. / 4. : 1.0 / PI_REF / hh * 21. / 16.;
-  k_p2g<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, Cw);
+  k_p2g<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, Cw, fresh_bins ? p2g_skip<D>(K) : 0);
+}
+
+/* the newly present phases k_p2g flagged (runs after it) */
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::p2g_new(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
+  const double hi = K.p_g * 1 * 3.2 / CUT_OFF;
+  double hh = (D == 2) ? hi * hi : hi * hi * hi;
+  double Cw = (D == 2) ? 1.0 / PI_REF / hh * 7. / 4. : 1.0 / PI_REF / hh * 21. / 16.;
   k_p2g_new<D, R, EX><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, Cw);
 }
 
@@ -1196,7 +1232,8 @@ void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out
 #define PGDG_INST(D, R, EX)                                                                     \
   template void Launch<D, R, EX>::used_state(const CaseK&, const DevPtrs<R>&, cudaStream_t);       \
   template void Launch<D, R, EX>::set_timestep(const CaseK&, const DevPtrs<R>&, int, cudaStream_t); \
-  template void Launch<D, R, EX>::p2g(const CaseK&, const DevPtrs<R>&, cudaStream_t);              \
+  template void Launch<D, R, EX>::p2g(const CaseK&, const DevPtrs<R>&, bool, cudaStream_t);        \
+  template void Launch<D, R, EX>::p2g_new(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \
   template void Launch<D, R, EX>::limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \
   template void Launch<D, R, EX>::grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);         \
   template int64_t Launch<D, R, EX>::iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t); \

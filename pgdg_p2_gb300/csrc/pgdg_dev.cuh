@@ -204,7 +204,10 @@ struct Launch {
   /* k_grid.cu */
   static void used_state(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void set_timestep(const CaseK&, const DevPtrs<R>&, int by_cells, cudaStream_t);
-  static void p2g(const CaseK&, const DevPtrs<R>&, cudaStream_t);
+  /* fresh_bins: every particle lies in its bucket's cell (right after
+   * binning), so neighbour cells beyond the cut radius can be skipped */
+  static void p2g(const CaseK&, const DevPtrs<R>&, bool fresh_bins, cudaStream_t);
+  static void p2g_new(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   /* queued variant: returns the number of interface problems (negative: over capacity) */

@@ -150,6 +150,7 @@ struct Ctx : pgdg_ctx {
   /* every particle lies in its bucket's cell (true from binning until the
    * particles move); P2G then skips neighbour cells beyond its cut radius */
   bool fresh_bins = false;
+  bool g2p_partial = false; /* see run_step */
   double *d_gam = nullptr, *d_pinf = nullptr;
   unsigned long long* d_ncell = nullptr;
 
@@ -886,7 +887,7 @@ struct Ctx : pgdg_ctx {
       xn = 3 - xs - x0b;
       if (xn == xs || xn == x0 || xn < 0 || xn > 2) xn = (xs + 1) % 3;  /* md 1 without md 0 */
     }
-    timed("g2p", 1, [&] { Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, st); });
+    timed("g2p", 1, [&] { Launch<D, R, EX>::g2p(K, P, md, xs, x0, xn, hn, !g2p_partial, st); });
     if (!EX) timed("rowsort", 3, [&] { Launch<D, R, EX>::rowsort(K, P, xs, pst_scratch, st); });
     if (pst_var < 0)
       pst_var = tune(Launch<D, R, EX>::pst_variants(),
@@ -909,7 +910,11 @@ struct Ctx : pgdg_ctx {
       limiter();
       grid_acc();
       update_grid(md);
+      /* inside a step, the first stage's G2P skips the fields the second
+       * stage's G2P rewrites before anything reads them */
+      g2p_partial = md == 0;
       update_particle(md);
+      g2p_partial = false;
     }
     return PGDG_OK;
   }

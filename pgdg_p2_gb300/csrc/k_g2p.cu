@@ -55,7 +55,7 @@ template <>
 __device__ __forceinline__ float hroot<3, float>(float vol) { return cbrtf(vol) * 3.2f / 2.f; }
 
 template <int D, typename R, bool EX>
-__global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPtrs<R> P, int md, int xs, int x0b, int xn, int hn) {
+__global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPtrs<R> P, int md, int xs, int x0b, int xn, int hn, int full) {
   constexpr int U = D + 2, B = D + 1;
   const int64_t n = (int64_t)P.cnt->n_slots;
   const int64_t nc = K.ncell;
@@ -117,9 +117,10 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPt
     R Pp = eos_p<R>(E - R(0.5) * rho * sq, g, pfe_r[ss]);
     R c = sqrt_r<R>(g * (pf + Pp) / rho);
     bool fb = (Pp < R(-0.05) * pf || rho < R(0));
-    for (int t = 0; t < U; t++)
-      for (int b = 0; b < D; b++)
-        P.sl[(t * D + b) * K.cap + p] = fb ? R(0) : P.ccoef[((ss * U + t) * B + 1 + b) * nc + ci];
+    if (full)
+      for (int t = 0; t < U; t++)
+        for (int b = 0; b < D; b++)
+          P.sl[(t * D + b) * K.cap + p] = fb ? R(0) : P.ccoef[((ss * U + t) * B + 1 + b) * nc + ci];
     if (fb) {
       rho = P.crho[ss * nc + ci];
       for (int k = 0; k < D; k++) rhov[k] = P.crhov[(ss * D + k) * nc + ci];
@@ -129,15 +130,17 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPt
     }
     for (int d = 0; d < D; d++) {
       XN[d * K.cap + p] = x[d];
-      P.rhov[d * K.cap + p] = rhov[d];
+      if (full) P.rhov[d * K.cap + p] = rhov[d];
       P.v[d * K.cap + p] = v[d];
     }
     P.vol[p] = vol;
     P.rho[p] = rho;
-    P.E[p] = E;
-    P.P[p] = Pp;
+    if (full) {
+      P.E[p] = E;
+      P.P[p] = Pp;
+      P.mass[p] = vol * rho;
+    }
     P.c[p] = c;
-    P.mass[p] = vol * rho;
     HN[p] = hroot<D, R>(vol);
     /* the shifting sum's record: position and volume, the phase in the
      * volume's sign (two phases), density and sound speed apart (read only
@@ -158,8 +161,9 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPt
 }
 
 template <int D, typename R, bool EX>
-void Launch<D, R, EX>::g2p(const CaseK& K, const DevPtrs<R>& P, int md, int xs, int x0, int xn, int hn, cudaStream_t st) {
-  k_g2p<D, R, EX><<<grid_for(K.cap, 128), 128, 0, st>>>(K, P, md, xs, x0, xn, hn);
+void Launch<D, R, EX>::g2p(const CaseK& K, const DevPtrs<R>& P, int md, int xs, int x0, int xn, int hn, bool full,
+                           cudaStream_t st) {
+  k_g2p<D, R, EX><<<grid_for(K.cap, 128), 128, 0, st>>>(K, P, md, xs, x0, xn, hn, full ? 1 : 0);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1370,7 +1374,8 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
 }
 
 #define PGDG_INST(D, R, EX)                                                                              \
-  template void Launch<D, R, EX>::g2p(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, cudaStream_t); \
+  template void Launch<D, R, EX>::g2p(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, bool,     \
+                                      cudaStream_t);                                                       \
   template void Launch<D, R, EX>::pst(const CaseK&, const DevPtrs<R>&, int, int, int, int, int, void*,        \
                                       cudaStream_t);                                                       \
   template size_t Launch<D, R, EX>::pst_scratch_bytes(const CaseK&);                                       \

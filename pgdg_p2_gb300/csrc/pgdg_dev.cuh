@@ -218,7 +218,10 @@ struct Launch {
   /* k_g2p.cu */
   /* xs/hs: stage-start coordinate/h buffers, x0: step-start coordinates (md 1),
    * xn/hn: buffers receiving the new coordinates/h */
-  static void g2p(const CaseK&, const DevPtrs<R>&, int md, int xs, int x0, int xn, int hn, cudaStream_t);
+  /* full = false: skip the slopes, energy, pressure, momentum and mass, which
+   * nothing reads before the next G2P of the same step rewrites them */
+  static void g2p(const CaseK&, const DevPtrs<R>&, int md, int xs, int x0, int xn, int hn, bool full,
+                  cudaStream_t);
   /* shifting: scratch holds pst_scratch_bytes(K) bytes of device memory */
   static void pst(const CaseK&, const DevPtrs<R>&, int xs, int hs, int xn, int hn, int var, void* scratch,
                   cudaStream_t);

@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(6)) k_limiter(CaseK K, D
             if (s1 != s) {
               R vj[3], sq = R(0);
               for (int k = 0; k < D; k++) {
-                vj[k] = rvj[k] / rhoj;
+                vj[k] = qdiv<R, EX>(rvj[k], rhoj);
                 sq = (k == 0) ? vj[k] * vj[k] : sq + vj[k] * vj[k];
               }
               R rhoe_j = Ej - R(0.5) * rhoj * sq;
@@ -620,8 +620,8 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(6)) k_limiter(CaseK K, D
           R dU = R(0);
           for (int b = 0; b < D; b++) dU = (b == 0) ? co[u][1 + b] * dr[b] : dU + co[u][1 + b] * dr[b];
           R sd = R(1);
-          if (dU >= R(0)) sd = limiter_fn<R>(fabs(u_max[s][u] / (dU + R(1e-20))), lim_fg);
-          else if (dU < R(0)) sd = limiter_fn<R>(fabs(u_min[s][u] / (dU + R(1e-20))), lim_fg);
+          if (dU >= R(0)) sd = limiter_fn<R>(fabs(qdiv<R, EX>(u_max[s][u], dU + R(1e-20))), lim_fg);
+          else if (dU < R(0)) sd = limiter_fn<R>(fabs(qdiv<R, EX>(u_min[s][u], dU + R(1e-20))), lim_fg);
           lim[s][u] = amin1(lim[s][u], sd);
         }
       }
@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(6)) k_limiter(CaseK K, D
         }
         R sq = Ui[1] * Ui[1];
         for (int k = 1; k < D; k++) sq = sq + Ui[1 + k] * Ui[1 + k];
-        R e_p = Ui[U - 1] - R(0.5) * sq / Ui[0];
+        R e_p = Ui[U - 1] - qdiv<R, EX>(R(0.5) * sq, Ui[0]);
         R P_p = eos_p<R>(e_p, gs, pfe);
         if (P_p < R(-0.05) * pf || Ui[0] < R(0)) fg = 1;
       }
@@ -751,8 +751,8 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
         R rho_p = Up[0];
         R vp[3], sq = Up[1] * Up[1];
         for (int k = 1; k < D; k++) sq = sq + Up[1 + k] * Up[1 + k];
-        for (int k = 0; k < D; k++) vp[k] = Up[1 + k] / rho_p;
-        R P_p = eos_p<R>(Up[U - 1] - R(0.5) * sq / rho_p, gs, pfe);
+        for (int k = 0; k < D; k++) vp[k] = qdiv<R, EX>(Up[1 + k], rho_p);
+        R P_p = eos_p<R>(Up[U - 1] - qdiv<R, EX>(R(0.5) * sq, rho_p), gs, pfe);
         for (int bi = 1; bi <= D; bi++) {
           R Fc[U];
           flux_col<D, R>(Up, vp, P_p, bi - 1, Fc, esh);
@@ -821,9 +821,9 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
           const R rho_i = Ui[0], E_i = Ui[U - 1];
           R v_i[3], sq = Ui[1] * Ui[1];
           for (int k = 1; k < D; k++) sq = sq + Ui[1 + k] * Ui[1 + k];
-          for (int k = 0; k < D; k++) v_i[k] = Ui[1 + k] / rho_i;
-          const R P_i = eos_p<R>(E_i - R(0.5) * sq / rho_i, gs, pfe);
-          const R c_i = sqrt_r<R>(gs * (pfs + P_i) / rho_i);
+          for (int k = 0; k < D; k++) v_i[k] = qdiv<R, EX>(Ui[1 + k], rho_i);
+          const R P_i = eos_p<R>(E_i - qdiv<R, EX>(R(0.5) * sq, rho_i), gs, pfe);
+          const R c_i = sqrt_r<R>(qdiv<R, EX>(gs * (pfs + P_i), rho_i));
           const R vni = pick<D, R>(v_i, a) * na;
           R Fi[U];
           flux_col<D, R>(Ui, v_i, P_i, a, Fi, esh);
@@ -861,7 +861,7 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
               R sqj = R(0);
               for (int k = 0; k < D; k++) {
                 rhov_j[k] = Uj[1 + k];
-                v_j[k] = rhov_j[k] / rho_j;
+                v_j[k] = qdiv<R, EX>(rhov_j[k], rho_j);
                 sqj = (k == 0) ? v_j[k] * v_j[k] : sqj + v_j[k] * v_j[k];
               }
               R rhoe_j = E_j - R(0.5) * sqj * rho_j;
@@ -906,7 +906,7 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
                 }
                 E_j = eos_rhoe<R>(P_j, gs, pfe) + R(0.5) * rho_j * sqj;
               }
-              const R c_j = sqrt_r<R>(gs * (pfs + P_j) / rho_j);
+              const R c_j = sqrt_r<R>(qdiv<R, EX>(gs * (pfs + P_j), rho_j));
               R Ujj[U];
               Ujj[0] = rho_j;
               for (int k = 0; k < D; k++) Ujj[1 + k] = rhov_j[k];
@@ -918,26 +918,26 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
               /* HLLC (particle_flow.cpp:232-272) */
               const R SL = amin1(vni2 - c_i, vnj - c_j);
               const R SR = amax1(vni2 + c_i, vnj + c_j);
-              const R S_s = ((P_j - P_i) + rho_i * vni2 * (SL - vni2) - rho_j * vnj * (SR - vnj)) /
-                            (rho_i * (SL - vni2) - rho_j * (SR - vnj));
+              const R S_s = qdiv<R, EX>((P_j - P_i) + rho_i * vni2 * (SL - vni2) - rho_j * vnj * (SR - vnj),
+                                        rho_i * (SL - vni2) - rho_j * (SR - vnj));
               R Fh[U];
               if (SL > R(0)) {
                 for (int u = 0; u < U; u++) Fh[u] = Fi[u];
               } else if (SL <= R(0) && S_s >= R(0)) {
-                const R rho_sL = rho_i * (SL - vni2) / (SL - S_s);
+                const R rho_sL = qdiv<R, EX>(rho_i * (SL - vni2), SL - S_s);
                 R UsL[U];
                 UsL[0] = rho_sL;
                 for (int k = 0; k < D; k++) UsL[1 + k] = rho_sL * (v_i[k] + (k == a ? (S_s - vni2) * na : R(0)));
-                UsL[U - 1] = rho_sL * (E_i / rho_i + (S_s - vni2) * (S_s + P_i / (rho_i * (SL - vni2))));
-                if (esh != R(0)) UsL[U - 1] += esh * ((S_s - vni2) / (SL - S_s));   /* esh (rho_star / rho - 1) */
+                UsL[U - 1] = rho_sL * (qdiv<R, EX>(E_i, rho_i) + (S_s - vni2) * (S_s + qdiv<R, EX>(P_i, rho_i * (SL - vni2))));
+                if (esh != R(0)) UsL[U - 1] += esh * qdiv<R, EX>(S_s - vni2, SL - S_s);   /* esh (rho_star / rho - 1) */
                 for (int u = 0; u < U; u++) Fh[u] = Fi[u] + SL * (UsL[u] - Ui[u]) * na;
               } else if (S_s <= R(0) && SR >= R(0)) {
-                const R rho_sR = rho_j * (SR - vnj) / (SR - S_s);
+                const R rho_sR = qdiv<R, EX>(rho_j * (SR - vnj), SR - S_s);
                 R UsR[U];
                 UsR[0] = rho_sR;
                 for (int k = 0; k < D; k++) UsR[1 + k] = rho_sR * (v_j[k] + (k == a ? (S_s - vnj) * na : R(0)));
-                UsR[U - 1] = rho_sR * (E_j / rho_j + (S_s - vnj) * (S_s + P_j / (rho_j * (SR - vnj))));
-                if (esh != R(0)) UsR[U - 1] += esh * ((S_s - vnj) / (SR - S_s));
+                UsR[U - 1] = rho_sR * (qdiv<R, EX>(E_j, rho_j) + (S_s - vnj) * (S_s + qdiv<R, EX>(P_j, rho_j * (SR - vnj))));
+                if (esh != R(0)) UsR[U - 1] += esh * qdiv<R, EX>(S_s - vnj, SR - S_s);
                 for (int u = 0; u < U; u++) Fh[u] = Fj[u] + SR * (UsR[u] - Ujj[u]) * na;
               } else if (SR <= R(0)) {
                 for (int u = 0; u < U; u++) Fh[u] = Fj[u];
@@ -985,7 +985,7 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
             Uj[0] = rho_j;
             for (int k = 0; k < D; k++) Uj[1 + k] = rhov_j[k];
             Uj[U - 1] = E_j;
-            const R c_j = sqrt_r<R>(gs * (pfs + P_j) / rho_j);
+            const R c_j = sqrt_r<R>(qdiv<R, EX>(gs * (pfs + P_j), rho_j));
             const R vnj = pick<D, R>(v_j, a) * na;
             R Fj[U];
             flux_col<D, R>(Uj, v_j, P_j, a, Fj, esh);
@@ -995,7 +995,7 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
             if (SL > R(0)) {
               for (int u = 0; u < U; u++) Fh[u] = Fi[u];
             } else if (SL <= R(0) && SR >= R(0)) {
-              for (int u = 0; u < U; u++) Fh[u] = (SR * Fi[u] - SL * Fj[u] + SL * SR * (Uj[u] - Ui[u]) * na) / (SR - SL);
+              for (int u = 0; u < U; u++) Fh[u] = qdiv<R, EX>(SR * Fi[u] - SL * Fj[u] + SL * SR * (Uj[u] - Ui[u]) * na, SR - SL);
             } else if (SR < R(0)) {
               for (int u = 0; u < U; u++) Fh[u] = Fj[u];
             } else {

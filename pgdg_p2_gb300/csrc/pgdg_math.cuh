@@ -96,6 +96,15 @@ PGDG_HD R eos_p(R ee, R g, R pinf) { return ee * (g - R(1)) - g * pinf; }
 template <typename R>
 PGDG_HD R eos_rhoe(R p, R g, R pinf) { return (p + g * pinf) / (g - R(1)); }
 
+/* quotient of the stage arithmetic: the FP32 path uses the fast division
+ * (within 2 ulp for divisors of normal magnitude), every other build the IEEE
+ * division, so the exact path is unchanged */
+template <typename R, bool EX>
+__device__ __forceinline__ R qdiv(R a, R b) {
+  if constexpr (!EX && sizeof(R) == 4) return __fdividef(a, b);
+  else return a / b;
+}
+
 template <typename R>
 PGDG_HD R sqrt_r(R x);
 template <>

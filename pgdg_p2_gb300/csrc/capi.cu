@@ -776,7 +776,7 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
   int split() override {
-    timed("split", 12, [&] { Launch<D, R, EX>::split(K, P, st); });
+    timed("split", 14, [&] { Launch<D, R, EX>::split(K, P, st); });
     return PGDG_OK;
   }
   int merge(bool chained = false) override {

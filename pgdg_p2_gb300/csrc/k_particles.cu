@@ -359,16 +359,29 @@ __global__ void k_split_flags(CaseK K, DevPtrs<R> P) {
       bool f3 = x0 > K.br[0];
       code = f1 ? 1 : (f2 ? 2 : (f3 ? 3 : 0));
       if (code == 3) atomicAdd(&P.cnt->step_new, 1ull); /* outlet count (step_new reused) */
+      if (code) atomicAdd(&P.cnt->split_events, 1ull);
     }
     P.evcode[p] = code;
     P.scan[p] = (code == 1) ? (1ull << 32) : (code == 2 ? 1ull : 0ull);
   }
 }
 
+/* the split's event sweeps cover all slots, or none when no particle has an
+ * event (split, inlet or outlet) this step */
+template <typename R>
+__global__ void k_split_begin(DevPtrs<R> P) {
+  P.cnt->split_events = 0;
+}
+template <typename R>
+__global__ void k_split_gate(DevPtrs<R> P) {
+  DevCounters* c = P.cnt;
+  c->split_n = c->split_events ? c->n_slots : 0ull;
+}
+
 template <int D, typename R>
 __global__ void k_split_emit(CaseK K, DevPtrs<R> P) {
   constexpr int CN = (D == 3) ? 8 : 4;
-  const int64_t n = (int64_t)P.cnt->n_slots;
+  const int64_t n = (int64_t)P.cnt->split_n;
   const unsigned long long tot = P.scan_blk[scan_nblk(K.cap)];
   const int64_t nsplit = (int64_t)(tot >> 32), ninlet = (int64_t)(tot & 0xffffffffull);
   if (n + (CN - 1) * nsplit + ninlet > K.cap) {
@@ -491,7 +504,7 @@ __global__ void k_split_finish(CaseK K, DevPtrs<R> P) {
 /* old neighbours of split parents (code 1) and outlet particles (code 3) */
 template <typename R>
 __global__ void k_aff_oldnbr_split(CaseK K, DevPtrs<R> P) {
-  const int64_t n = (int64_t)P.cnt->n_slots;
+  const int64_t n = (int64_t)P.cnt->split_n;
   GRID_STRIDE(p, n) {
     int code = P.evcode[p];
     if (code != 1 && code != 3) continue;
@@ -644,8 +657,10 @@ __global__ void k_reset_queues(DevPtrs<R> P) {
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::split(const CaseK& K, const DevPtrs<R>& P, cudaStream_t st) {
   const int g = grid_for(K.cap, BLK);
+  k_split_begin<R><<<1, 1, 0, st>>>(P);
   k_split_flags<D, R><<<g, BLK, 0, st>>>(K, P);
-  scan_u64(P.scan, P.scan_blk, &P.cnt->n_slots, K.cap, st);
+  k_split_gate<R><<<1, 1, 0, st>>>(P);
+  scan_u64(P.scan, P.scan_blk, &P.cnt->split_n, K.cap, st);
   k_aff_oldnbr_split<R><<<g, BLK, 0, st>>>(K, P);
   k_split_emit<D, R><<<g, BLK, 0, st>>>(K, P);
   k_split_finish<D, R><<<1, 1, 0, st>>>(K, P);

@@ -52,6 +52,8 @@ struct DevCounters {
   unsigned long long queue_n;
   unsigned long long merge_n;     /* slots the current merge pass sweeps */
   unsigned long long merge_quiet; /* the last merge pass merged nothing */
+  unsigned long long split_events; /* particles with a split, inlet or outlet event */
+  unsigned long long split_n;      /* slots the split's event sweeps cover */
   unsigned int err;
   unsigned int pad;
   double dt, max_v;

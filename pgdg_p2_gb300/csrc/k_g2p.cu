@@ -171,14 +171,20 @@ void Launch<D, R, EX>::g2p(const CaseK& K, const DevPtrs<R>& P, int md, int xs, 
 /* ------------------------------------------------------------------ */
 /* One CTA per brick of cells.  The CTA stages the stage-start position and slot
  * of every particle in the brick's +-rad2 neighbourhood into shared memory as one
- * 16-byte (FP32) or 32-byte (FP64) entry, together with per-cell list offsets,
- * the exact bounding box of each cell's entries and a boundary-particle flag.
- * Each thread then scans one particle's candidates from shared memory, queues
- * the members in scan order and sums their contributions in warp-wide batches
- * (a warp vote flushes every queue together, so the pair arithmetic runs with
- * full warps).  A particle whose scan range leaves the staged box (it crossed a
- * cell face during the first stage) reads global memory instead, in the same
- * order, so both paths give the same result. */
+ * 16-byte (FP32) or 32-byte (FP64) entry, with a boundary-particle flag per cell.
+ *   - Mixed and FMA paths: per row of cells along the last axis, the CTA copies
+ *     the contiguous range of that row's entries sorted by the last-axis
+ *     coordinate (the per-stage row sort), tags each entry with its cell's
+ *     offset in the row window and reduces the row's bounds in the other axes.
+ *     Each thread then takes one particle: per row, a binary search finds the
+ *     chord of its 2h sphere, the cell tag keeps the reference's +-rad2 window,
+ *     and members are summed at once (or queued, variant 0) in sorted order.
+ *   - Exact path: per-cell list offsets, the exact bounding box of each cell's
+ *     entries and the reference's list order (binned entries, boundary
+ *     particles, appended entries), scanned cell by cell.
+ * A particle whose scan range leaves the staged box (it crossed a cell face
+ * during the first stage) reads global memory instead, in the reference's list
+ * order. */
 template <int D>
 struct Brick;
 template <>
@@ -1316,8 +1322,9 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
   k_pst<D, R, EX, VAR><<<nbx * nb1 * nb0, pst_threads(VAR), bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap, RS);
 }
 
-/* variants of the shifting kernel (identical results; the context's autotuner
- * times them on its own state and keeps the fastest): 0 per-lane row scan with
+/* variants of the shifting kernel (the same members; results equal to rounding,
+ * since variant 1 sums boundary particles in a second pass; the context's
+ * autotuner times them on its own state and keeps the fastest): 0 per-lane row scan with
  * queued members, 1 warp-cooperative row scan, 2 per-lane scan summing members
  * at once, 3 the same for 3 blocks per SM, 4 direct sums over bricks of twice
  * the cells with 512 threads, 5 over bricks of four times the cells with 1024

@@ -40,7 +40,11 @@ int pgdg_case_particles(const pgdg_case* cs, int config_id, uint64_t seed, pgdg_
 int pgdg_case_cells(const pgdg_case* cs, pgdg_cells* out);
 
 /* ---- context ---- */
-/* MPM::MPM + allocation; capacity = max fluid particles held (0 = automatic) */
+/* MPM::MPM + allocation; capacity = max fluid particles held (0 = automatic).
+ * PGDG_EINVAL without touching the GPU for a case it cannot hold: a cell count
+ * below 1 on an axis, or (MIXED and FP64_FMA, whose shifting kernel sorts
+ * each row of cells with 16-bit cell offsets) more than 65535 cells along the
+ * last axis. */
 int pgdg_create(const pgdg_case* cs, int precision, int64_t capacity, pgdg_ctx** out);
 int pgdg_destroy(pgdg_ctx* ctx);
 const char* pgdg_last_error(pgdg_ctx* ctx);
@@ -140,7 +144,10 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
  * PGDG_MGFM_NOALLOC_MAX entries (8 MiB); a larger n returns PGDG_EOVERFLOW
  * before anything is launched.  Nothing in that array is read before it is
  * written, so nothing is cleared.  The first call on a device looks the array
- * up (cudaGetSymbolAddress) and should come before any stream capture.
+ * up (cudaGetSymbolAddress) and should come before any stream capture.  The
+ * address is kept for the life of the process: do not call this entry point
+ * again on a device after cudaDeviceReset (or any other teardown of its
+ * primary context) in the same process.
  * Overlapping calls on one device (several host threads, or per-thread default
  * streams) share the array and race: serialise them.  A tensor-core network
  * (pgdg_surrogate_create mode 2) is refused (PGDG_EINVAL): its seeds differ from
@@ -164,7 +171,11 @@ int pgdg_set_graphs(pgdg_ctx* ctx, int on);
  * context times them on its own state at their first call and keeps the
  * fastest.  kernel: "pst" (the shifting kernel of pgdg_update_particle).
  * variant >= 0 forces that variant, -1 re-tunes at the next call, -2 only
- * queries; *chosen (may be NULL) receives the current choice (-1: not tuned). */
+ * queries; *chosen (may be NULL) receives the current choice (-1: not tuned).
+ * kernel "p2g_skip": 1 (default) lets pgdg_mls_p2g skip neighbour cells beyond
+ * its cut radius while every particle still lies in its bucket's cell (from
+ * pgdg_bin_particles until particles move); 0 always visits all 3^d cells.
+ * Both give identical sums. */
 int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen);
 
 /* ---- measurement ----

@@ -1,6 +1,6 @@
 """Build recipe for the CPU oracle (test infrastructure).
 
-Compiles oracle/pgdg_oracle.cpp with g++ into oracle/_build/liboracle.so.
+Compiles oracle/pgdg_oracle.cpp and oracle/oracle_case.cpp with g++ into oracle/_build/liboracle.so.
 -ffp-contract=off keeps every expression in written order with one rounding per
 operation on both x86_64 and aarch64 (where GCC would otherwise contract into FMA).
 """
@@ -11,7 +11,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SRCS = [os.path.join(HERE, "pgdg_oracle.cpp")]
+SRCS = [os.path.join(HERE, "pgdg_oracle.cpp"), os.path.join(HERE, "oracle_case.cpp")]
 DEPS = SRCS + [os.path.join(HERE, "oracle_math.h"), os.path.join(HERE, "pgdg_oracle.h"),
                os.path.join(HERE, "..", "include", "pgdg_types.h")]
 

@@ -56,12 +56,43 @@ def lib():
                                       P(C.c_double), P(C.c_double), P(C.c_int32), C.c_int64]
         L.po_root_d.argtypes = [C.c_double, C.c_int]
         L.po_root_d.restype = C.c_double
+        L.po_case_setup.argtypes = [C.c_int, P(C.c_int32), P(pgdg_case)]
+        L.po_case_num_particles.argtypes = [P(pgdg_case)]
+        L.po_case_num_particles.restype = C.c_int64
+        L.po_case_particles.argtypes = [P(pgdg_case), C.c_int, C.c_uint64, P(pgdg_particles)]
+        L.po_case_cells.argtypes = [P(pgdg_case), P(pgdg_cells)]
         _lib = L
     return _lib
 
 
 def set_threads(n):
     lib().po_set_threads(int(n))
+
+
+def case_setup(config_id, ncell=None):
+    """The oracle's own pgdg_case of workload config_id (grid override ncell)."""
+    cs = pgdg_case()
+    nc = (C.c_int32 * 3)(*(ncell or (0, 0, 0)))
+    check(lib().po_case_setup(int(config_id), nc, C.byref(cs)), "po_case_setup")
+    return cs
+
+
+def case_particles(cs, config_id, seed=0):
+    p = Particles(lib().po_case_num_particles(C.byref(cs)), cs.dim)
+    check(lib().po_case_particles(C.byref(cs), int(config_id), int(seed), C.byref(p.view())), "po_case_particles")
+    return p
+
+
+def case_cells(cs):
+    c = Cells(cs.ncells, cs.dim)
+    check(lib().po_case_cells(C.byref(cs), C.byref(c.view())), "po_case_cells")
+    return c
+
+
+def make_case(config_id, ncell=None, seed=0):
+    """(case, particles, cells) built by the oracle alone, without the GPU library."""
+    cs = case_setup(config_id, ncell)
+    return cs, case_particles(cs, config_id, seed), case_cells(cs)
 
 
 class Oracle:

@@ -21,6 +21,13 @@ extern "C" {
 
 typedef struct po_ctx po_ctx;
 
+/* the oracle's own construction of the synthetic workloads (oracle_case.cpp),
+ * bit-identical to pgdg_case_setup / _particles / _cells of the GPU library */
+int po_case_setup(int config_id, const int32_t* ncell, pgdg_case* out);
+int64_t po_case_num_particles(const pgdg_case* cs);
+int po_case_particles(const pgdg_case* cs, int config_id, uint64_t seed, pgdg_particles* out);
+int po_case_cells(const pgdg_case* cs, pgdg_cells* out);
+
 int po_create(const pgdg_case* cs, po_ctx** out);
 int po_destroy(po_ctx* ctx);
 int po_set_threads(int n);

@@ -24,7 +24,6 @@ CU = [("k_particles.cu", "k_particles", ["-fmad=false"]),
       ("k_grid.cu", "k_grid_x", ["-fmad=false", "-DPGDG_EXACT_TU"]),
       ("k_g2p.cu", "k_g2p", []),
       ("k_g2p.cu", "k_g2p_x", ["-fmad=false", "-DPGDG_EXACT_TU"]),
-      ("k_mgfm.cu", "k_mgfm", ["-fmad=false"]),
       ("k_mlp.cu", "k_mlp", ["-fmad=false"]),
       ("k_xfer.cu", "k_xfer", []),
       ("k_mlp_tc.cu", "k_mlp_tc", []),

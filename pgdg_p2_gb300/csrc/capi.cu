@@ -29,6 +29,7 @@ struct pgdg_ctx {
   void* net = nullptr;   /* attached seed surrogate (pgdg_mlp) */
   int iface_queue = 0;   /* 1: interface problems solved as one batch */
   int pst_var = -1;      /* shifting-kernel variant (-1: tune at the next call) */
+  int p2g_skip = 1;      /* 1: P2G skips out-of-reach neighbour cells while the bins are fresh */
   int64_t iface_last = 0;
   virtual int iface_download(double*, int8_t*, int64_t, int64_t*) = 0;
   /* captured step graphs (advance): dropped when what they bake in changes */
@@ -790,7 +791,7 @@ struct Ctx : pgdg_ctx {
    * the shifting kernel; nothing to do here */
   int refresh_neighbors() override { return PGDG_OK; }
   int p2g() override {
-    timed("p2g", 1, [&] { Launch<D, R, EX>::p2g(K, P, fresh_bins, st); });
+    timed("p2g", 1, [&] { Launch<D, R, EX>::p2g(K, P, fresh_bins && p2g_skip, st); });
     timed("p2g_new", 1, [&] { Launch<D, R, EX>::p2g_new(K, P, st); });
     return PGDG_OK;
   }
@@ -1023,6 +1024,15 @@ int pgdg_create(const pgdg_case* cs, int precision, int64_t capacity, pgdg_ctx**
   if (!cs || !out || cs->nfld != 2 || (cs->dim != 2 && cs->dim != 3)) return PGDG_EINVAL;
   if (precision != PGDG_PREC_FP64 && precision != PGDG_PREC_MIXED && precision != PGDG_PREC_FP64_FMA)
     return PGDG_EINVAL;
+  for (int d = 0; d < cs->dim; d++)
+    if (cs->ncell[d] < 1) return PGDG_EINVAL;
+  /* the shifting kernel's row sort (mixed and FP64_FMA paths) stores each
+   * entry's cell offset within its row in 16 bits */
+  if (precision != PGDG_PREC_FP64 && cs->ncell[cs->dim - 1] > 65535) {
+    fprintf(stderr, "pgdg_create: %d cells along the last axis; the row sort of this precision holds at most 65535\n",
+            cs->ncell[cs->dim - 1]);
+    return PGDG_EINVAL;
+  }
   int dev = 0;
   if (cudaGetDeviceCount(&dev) != cudaSuccess || dev < 1) return PGDG_ECUDA;
   pgdg_ctx* c;
@@ -1091,8 +1101,14 @@ int pgdg_set_graphs(pgdg_ctx* ctx, int on) {
   return PGDG_OK;
 }
 int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen) {
+  if (kernel && std::strcmp(kernel, "p2g_skip") == 0 && variant >= -2 && variant <= 1) {
+    if (variant >= 0) ctx->p2g_skip = variant;
+    if (variant >= 0) ctx->invalidate_graphs();
+    if (chosen) *chosen = ctx->p2g_skip;
+    return PGDG_OK;
+  }
   if (!kernel || std::strcmp(kernel, "pst") != 0 || variant < -2) {
-    ctx->err = "tunable kernels: pst; variant >= -2";
+    ctx->err = "tunable kernels: pst (variant >= -2), p2g_skip (0, 1, or -2 to query)";
     return PGDG_EINVAL;
   }
   if (variant >= 0) ctx->pst_var = variant;

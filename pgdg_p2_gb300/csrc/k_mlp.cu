@@ -412,8 +412,11 @@ __global__ void k_mgfm_seeded(const double* __restrict__ in6, const int8_t* __re
                               const double* __restrict__ seed, double* __restrict__ out3, int32_t* __restrict__ iters,
                               int64_t n, unsigned long long* stats, const float* __restrict__ Y,
                               const float* __restrict__ sc, const float* __restrict__ params,
-                              const int32_t* __restrict__ perm) {
+                              const int32_t* __restrict__ perm, const int* __restrict__ yerr) {
   unsigned long long nit = 0, nmax = 0, ncall = 0;
+  /* a tensor-core forward pass that gave up leaves Y unset: every problem then
+   * starts from the plain seed (the reference's), so results stay valid */
+  if (yerr && *yerr) Y = nullptr;
   const float my0 = params ? params[NPARAM + 2 * NI] : 0.f, sy0 = params ? params[NPARAM + 2 * NI + NO] : 1.f;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = perm ? (int64_t)perm[j] : j;
@@ -425,6 +428,7 @@ __global__ void k_mgfm_seeded(const double* __restrict__ in6, const int8_t* __re
      * scale and the network output */
     double sd = seed ? seed[i] : -1.0;
     if (Y && sd > 0) sd = seed_value(sd, sc[i], Y[i * NO], my0, sy0);
+    else if (seed && !Y && yerr) sd = -1.0;
     bool done = false;
     if (sd > 0) {
       it = mgfm(q[0], q[1], q[2], q[3], q[4], q[5], gam[s], pinf[s], gam[s1], pinf[s1], variant, sd, o);
@@ -512,6 +516,8 @@ inline int g_for(int64_t n, int b) {
 }
 void forward(pgdg_mlp* m, const float* X, float* Y, float* A1, float* A2, float* A3, int64_t n, cudaStream_t st) {
   if (m->tc && !A1) {
+    /* the flag reports this forward pass only */
+    cudaMemsetAsync(m->d_tcerr, 0, sizeof(int), st);
     mlp_tc_forward(m->d_params, X, Y, n, m->d_tcerr, st);
     return;
   }
@@ -688,7 +694,7 @@ int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8
     sd = seeds;
   }
   k_mgfm_seeded<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, nullptr, nullptr, nullptr,
-                                        nullptr, nullptr);
+                                        nullptr, nullptr, nullptr);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 
@@ -752,7 +758,7 @@ int mgfm_seeded_run(void* netv, const double* in6, const int8_t* mat2, const dou
   k_root_perm<<<g_for(n, 256), 256, 0, st>>>(ps.pos, ps.blk + (n + 2047) / 2048, ps.perm, n);
   k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, stats,
                                                m ? m->Y : nullptr, m ? m->sc : nullptr, m ? m->d_params : nullptr,
-                                               ps.perm);
+                                               ps.perm, m && m->tc ? m->d_tcerr : nullptr);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 }  // namespace pgdg

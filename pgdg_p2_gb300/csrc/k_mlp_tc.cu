@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_tc(const float* __restrict__ par
 
   const uint32_t id64 = idesc_bf16(TILE, NH_), id16 = idesc_bf16(TILE, N4);
   const uint64_t dA0 = sdesc(sbase + S_A0, 128, (K1 / 8) * 128), dW1 = sdesc(sbase + S_W1, 128, (K1 / 8) * 128);
-  uint32_t phase = 0;
+  uint32_t phase = 0, pend = 0;
   bool ok = true;
   const int64_t ntile = (n + TILE - 1) / TILE;
   for (int64_t tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
@@ -243,6 +243,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_tc(const float* __restrict__ par
         mma_commit(mbar);
       }
       ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+      pend = phase;
       phase ^= 1u;
       if (!ok) break;
       fence_after();
@@ -262,7 +263,14 @@ __global__ void __launch_bounds__(128, 4) k_mlp_tc(const float* __restrict__ par
     fence_before();
     __syncthreads();
   }
-  if (!ok && t == 0) atomicExch(err, 1);
+  if (!ok) {
+    /* a wait gave up: flag the launch (its outputs, and anything later on the
+     * stream that reads them, are invalid), issue no further MMA, and give the
+     * last commit one more bounded wait so that its MMA no longer writes the
+     * tensor memory or arrives on the barrier once both are released */
+    if (t == 0) atomicExch(err, 1);
+    (void)mbar_wait(mbar, pend);
+  }
   fence_before();
   __syncthreads();
   fence_after();

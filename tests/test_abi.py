@@ -68,3 +68,21 @@ int main(void) {
            ctypes.sizeof(abi.pgdg_stats), abi.pgdg_case.probe.offset, abi.pgdg_case.cfl.offset,
            abi.pgdg_cells.dcoef.offset]
     assert out == exp
+
+
+def test_create_rejects_rows_beyond_16_bit_offsets():
+    # the mixed and FP64_FMA shifting kernel sorts each row of cells along the
+    # last axis with 16-bit cell offsets: a longer last axis is refused before
+    # any GPU call (so this runs without a GPU); the exact path has no row sort
+    import ctypes as C
+    from pgdg_p2_gb300.abi import PREC_MIXED
+    lib = mpm.lib()
+    for dim, grid in ((2, (4, 65536)), (3, (2, 2, 70000))):
+        cs = mpm.case_setup(1 if dim == 2 else 3, (8, 4) if dim == 2 else (8, 4, 4))
+        for d in range(dim):
+            cs.ncell[d] = grid[d]
+        h = C.c_void_p()
+        for prec in (PREC_MIXED, 2):
+            assert lib.pgdg_create(C.byref(cs), prec, 0, C.byref(h)) == -1
+        cs.ncell[dim - 1] = 0
+        assert lib.pgdg_create(C.byref(cs), 0, 0, C.byref(h)) == -1

@@ -62,3 +62,25 @@ def test_undex_stiffened_gas():
     water = p.phase == 1
     assert cs.pinf[0] == 3.309e8 and cs.gamma[0] == 7.15
     assert np.allclose(p.c[water], math.sqrt(7.15 * (1e5 + 3.309e8) / 1000))
+
+
+@pytest.mark.parametrize("cid,grid,seed", [(1, None, 0), (1, (56, 24), 77), (2, (32, 8, 8), 0), (3, (48, 12, 12), 0),
+                                           (3, (96, 24, 24), 0), (4, (64, 64), 0), (2, None, 0), (3, None, 0),
+                                           (4, None, 0)])
+def test_oracle_case_builder_bitwise(cid, grid, seed):
+    """The oracle's own case construction (used by the CPU arms of the bench,
+    which load no GPU library) equals the library's bit for bit: the case
+    parameters always, particles and cells where the case fits a CPU test."""
+    from oracle import oracle as O
+    cs_g, cs_o = M.case_setup(cid, grid), O.case_setup(cid, grid)
+    assert bytes(cs_g) == bytes(cs_o)
+    if grid is None and cid != 1:
+        return
+    pg, po = M.case_particles(cs_g, cid, seed), O.case_particles(cs_o, cid, seed)
+    assert pg.n == po.n
+    for k in pg.NAMES:
+        assert getattr(pg, k).tobytes() == getattr(po, k).tobytes(), k
+    cg, co = M.case_cells(cs_g), O.case_cells(cs_o)
+    for k in ("rho", "rhov", "E", "c", "ac", "alph", "coef", "v", "P", "ph_state", "ph_state_b", "used", "lim_u",
+              "g_v", "dcoef"):
+        assert getattr(cg, k).tobytes() == getattr(co, k).tobytes(), k

@@ -38,6 +38,9 @@ WORKLOADS = {
 }
 CONFIG_ID = 3
 WORKLOAD, GRID, SAMPLE_GRID = WORKLOADS[CONFIG_ID]
+# DRAM bytes read + written per particle by one shifting launch (ncu capture of
+# the 192x48x48 sphere: 429.4 MB for 3,538,944 particles)
+PST_TRAFFIC_PER_PARTICLE = 429.4e6 / 3538944
 
 
 def _dist():
@@ -114,44 +117,150 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def cpu_baseline(steps=1, warmup=1, threads=None):
-    """The CPU restatement (oracle) timed on a bounded sample of the same case."""
-    from oracle import oracle as O
-    from pgdg_p2_gb300 import mpm as M
-    threads = threads or os.cpu_count()
-    O.set_threads(threads)
-    cs, p, c = M.make_case(CONFIG_ID, SAMPLE_GRID)
-    o = O.Oracle(cs)
-    o.upload_particles(p)
-    o.upload_cells(c)
-    o.advance(warmup)
-    t0 = time.perf_counter()
-    o.advance(steps)
-    dt = time.perf_counter() - t0
-    ncell = cs.ncells
-    return {"value": ncell * 2 * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"same case on {SAMPLE_GRID[0]}x{SAMPLE_GRID[1]}x{SAMPLE_GRID[2]} cells "
-                      f"({p.n} particles), {steps} step(s) after {warmup} warm-up, FP64 CPU oracle "
-                      f"(OpenMP, {threads} threads); reference build unavailable (Eigen/oneTBB/Boost.MPI/MPI absent)",
-            "seconds": dt}
+# through-interaction accuracy runs on the bounded sample grid: steps that take
+# each workload well past its first interaction (the C3 sample meets the bubble
+# near step 96), and the steps of its bounded CPU-baseline timing
+SAMPLE_STEPS = {1: 200, 2: 130, 3: 130, 4: 120}
+# simulated time the full-size state is advanced to before the timed steps: the
+# shock reaches the bubble at t ~ 0.17 in both 3D shock-bubble cases
+REGIME_T = {1: 0.0, 2: 0.2, 3: 0.2, 4: 0.0}
+
+
+def host_mem_available():
+    """Bytes of host memory available (MemAvailable), or None when unknown."""
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except Exception:
+        pass
+    return None
+
+
+def oracle_bytes(n_particles, ncells):
+    """Host memory of the FP64 oracle holding a case: about 600 B of particle
+    state and neighbour lists per particle at 8 per cell, 1.7 kB per cell, and
+    the host arrays the case is built in."""
+    return int(n_particles * 900 + ncells * 2500)
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: the FP64 CPU oracle (the
+    reference itself cannot be built here), through its own case builder and
+    library only, on the full configuration when the host memory allows."""
     ws, rank, local = _dist()
     if rank != 0:
         return
-    # K steps and W warm-ups of the bounded sample (one sample step takes well
-    # under a second on the host cores)
-    cb = cpu_baseline(steps=args.steps, warmup=args.warmup)
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * cb["seconds"] / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample_grid": list(SAMPLE_GRID)},
-            "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"]},
-            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    from oracle import oracle as O
+    threads = os.cpu_count()
+    O.set_threads(threads)
+    cs = O.case_setup(CONFIG_ID, None)
+    grid, note = GRID, ""
+    need = oracle_bytes(O.lib().po_case_num_particles(O.C.byref(cs)), cs.ncells)
+    avail = host_mem_available()
+    if avail is not None and avail < 2 * need:
+        grid = SAMPLE_GRID
+        note = (f"; host memory available {avail / 2**30:.0f} GiB < 2 x {need / 2**30:.0f} GiB the full case needs, "
+                f"so the bounded sample grid ran")
+    cs, p, c = O.make_case(CONFIG_ID, grid)
+    o = O.Oracle(cs)
+    o.upload_particles(p)
+    o.upload_cells(c)
+    npart, ncell = p.n, cs.ncells
+    del p, c
+    o.advance(args.warmup)
+    t0 = time.perf_counter()
+    o.advance(args.steps)
+    dt = time.perf_counter() - t0
+    value = ncell * 2 * args.steps / dt
+    gl = "x".join(str(x) for x in grid[:cs.dim])
+    sample = (f"{'full configuration' if grid == GRID else 'bounded sample'}: {gl} cells ({npart} particles), "
+              f"{args.steps} step(s) timed after {args.warmup} warm-up step(s), FP64 CPU oracle (restatement of the "
+              f"reference's algorithm; OpenMP, {threads} threads; the reference itself needs Eigen, oneTBB, "
+              f"Boost.MPI and MPI, none installed){note}")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": list(grid[:cs.dim]), "same_config": grid == GRID},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def accuracy_sample(M, S, net, steps):
+    """The learned+mixed path and the plain FP64 GPU path against the FP64
+    oracle on the bounded sample grid, through the interaction: relative L1
+    per conserved variable (sum |q - q_oracle| / sum |q_oracle| over cells), the
+    oracle's own sensitivity to FP32-sized changes of the initial energies (the
+    floor a path that stores its state in FP32 meets), and the oracle's host
+    time over the same steps (the CPU baseline)."""
+    import numpy as np
+    from oracle import oracle as O
+    from pgdg_p2_gb300.abi import PREC_FP64_FMA, PREC_MIXED
+    threads = os.cpu_count()
+    O.set_threads(threads)
+    cs, p, c = O.make_case(CONFIG_ID, SAMPLE_GRID)
+    o, ob = O.Oracle(cs), O.Oracle(cs)
+    # the floor: the oracle from energies scaled by 1 +- 2^-24 (seeded signs), the
+    # size of rounding the state to FP32
+    q = p.copy()
+    q.E[:] = q.E * (1.0 + np.random.default_rng(12345).choice([-1.0, 1.0], size=q.E.shape) * 2.0 ** -24)
+    o.upload_particles(p)
+    ob.upload_particles(q)
+    paths = {"mixed_learned": M.MPM(cs, PREC_MIXED), "fp64": M.MPM(cs, PREC_FP64_FMA)}
+    paths["mixed_learned"].set_surrogate(net)
+    for g in paths.values():
+        g.upload_particles(p)
+    for x in (o, ob, *paths.values()):
+        x.upload_cells(c)
+    t_oracle, t_sim = 0.0, 0.0
+    for s in range(1, steps + 1):
+        t0 = time.perf_counter()
+        dt, mv = o.Set_timestep()
+        o.set_iterate(s)
+        o.MPM_run_simulation(s)
+        t_oracle += time.perf_counter() - t0
+        t_sim += dt
+        for x in (ob, *paths.values()):
+            x.Set_timestep()
+            x.set_dt(dt)
+            x.set_max_v(mv)
+            x.set_iterate(s)
+            x.MPM_run_simulation(s)
+
+    def l1(cg, co):
+        U = cs.dim + 2
+        mag = sum(np.abs((co.alph * co.coef[:, :, 1 + k, 0]).sum(1)).sum() for k in range(cs.dim))
+        per, mom = [], []
+        for u in range(U):
+            a = (cg.alph * cg.coef[:, :, u, 0]).sum(1)
+            b = (co.alph * co.coef[:, :, u, 0]).sum(1)
+            per.append(float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300)))
+            if 1 <= u <= cs.dim:
+                mom.append(float(np.abs(a - b).sum() / max(mag, 1e-300)))
+        return per, mom
+    co = o.download_cells()
+    floor, floor_m = l1(ob.download_cells(), co)
+    so = o.stats()
+    out = {"grid": list(SAMPLE_GRID[:cs.dim]), "steps": steps, "t": t_sim,
+           "variables": ["rho", "rho u", "rho v", "rho w", "E"] if cs.dim == 3 else ["rho", "rho u", "rho v", "E"],
+           "floor_l1": floor, "floor_momentum_over_sum_abs_rho_u": floor_m,
+           "oracle": {k: so[k] for k in ("n_split", "n_merge", "n_inlet", "n_outlet", "mgfm_calls", "mgfm_iters")}}
+    for name, g in paths.items():
+        g.sync()
+        per, mom = l1(g.download_cells(), co)
+        sg = g.stats()
+        out[name] = {"l1": per, "momentum_over_sum_abs_rho_u": mom,
+                     "within_1e-3_or_3x_floor": all(e <= max(1e-3, 3 * f) for e, f in zip(per, floor)),
+                     "stats": {k: sg[k] for k in ("n_split", "n_merge", "mgfm_calls", "mgfm_iters")}}
+        g.close()
+    gl = "x".join(str(x) for x in SAMPLE_GRID[:cs.dim])
+    cpu = {"value": cs.ncells * 2 * steps / t_oracle, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"same case on {gl} cells ({p.n} particles), the {steps} steps from t = 0 through the "
+                     f"shock-bubble interaction (t = {t_sim:.3f}), FP64 CPU oracle (OpenMP, {threads} threads); "
+                     f"reference build unavailable (Eigen/oneTBB/Boost.MPI/MPI absent)",
+           "seconds": t_oracle}
+    return out, cpu
 
 
 def pinned_alloc():
@@ -176,6 +285,25 @@ def state_bytes(p, c):
     return tot
 
 
+def evolve(g, t_end, chunk=25):
+    """Untimed set-up: advance the context until its simulated time reaches
+    t_end (the state the timed steps start from)."""
+    t0 = time.perf_counter()
+    n = 0
+    while g.stats()["time"] < t_end:
+        g.advance(chunk)
+        n += chunk
+    g.sync()
+    return {"t": g.stats()["time"], "steps": n, "seconds": time.perf_counter() - t0}
+
+
+def totals_drift(a, b):
+    """Relative change of the conservation totals between two pgdg_totals reads
+    (particle mass per phase, particle energy, cell mass per phase, cell energy)."""
+    names = ("particle_mass_1", "particle_mass_2", "particle_energy", "cell_mass_1", "cell_mass_2", "cell_energy")
+    return {k: float((b[i] - a[i]) / abs(a[i])) if a[i] != 0 else 0.0 for i, k in enumerate(names)}
+
+
 def run_ours(args):
     ws, rank, local = _dist()
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
@@ -197,7 +325,6 @@ def run_ours(args):
     if params is None:
         raise SystemExit("trained seed weights missing (python -m pgdg_p2_gb300.train_surrogate)")
     net = S.Surrogate(params, tc=True)
-
     grid = tuple(int(x) for x in args.grid.split(",")) if args.grid else GRID
     cs, p, c = M.make_case(CONFIG_ID, grid)
     ncell = cs.ncells
@@ -205,6 +332,17 @@ def run_ours(args):
     g.set_surrogate(net)
     g.upload_particles(p)
     g.upload_cells(c)
+    del p, c
+
+    # ---- untimed set-up: the state enters the shock-bubble interaction ----
+    t_reg = REGIME_T[CONFIG_ID] if args.regime_t < 0 else args.regime_t
+    regime = evolve(g, t_reg) if t_reg > 0 else {"t": 0.0, "steps": 0, "seconds": 0.0}
+    it_reg = g.stats()["iterate_num"]
+    pin = pinned_alloc()
+    np_reg = g.num_particles()
+    ph = M.Particles(np_reg + np_reg // 4 + 4096, cs.dim, alloc=pin)
+    g.download_particles(out=ph)
+    ch = g.download_cells(out=M.Cells(ncell, cs.dim, alloc=pin))
     g.advance(args.warmup)
     g.sync()
 
@@ -214,6 +352,7 @@ def run_ours(args):
             dist.barrier()
 
     # ---- timed region: K steps, CUDA events on the context stream ----
+    st0, tot0 = g.stats(), g.totals()
     barrier()
     n0 = g.launch_count()
     g.profile(True)
@@ -224,40 +363,40 @@ def run_ours(args):
     launches = g.launch_count() - n0
     barrier()
     ms, value = replica_value(ms, ncell, args.steps)
-    st = g.stats()
+    st, tot1 = g.stats(), g.totals()
+    window = {k: st[k] - st0[k] for k in ("n_split", "n_merge", "n_inlet", "n_outlet", "mgfm_calls", "mgfm_iters",
+                                           "mgfm_maxit_hits", "g2p_fallbacks")}
+    window["mgfm_iters_per_call"] = window["mgfm_iters"] / max(window["mgfm_calls"], 1)
+    window["t_start"], window["t_end"] = st0["time"], st["time"]
 
     if args.only_timed:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms / args.steps,
                               "gpu_launches": launches, "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
-                              "tuning": {"pst_variant": g.tune("pst")},
+                              "tuning": {"pst_variant": g.tune("pst")}, "regime": regime, "window": window,
                               "note": "timed region only"}), flush=True)
         g.close()
         return
 
     # ---- end to end through the C ABI with host buffers in page-locked memory ----
+    # the same regime state, uploaded from the host each time: K x (advance(1) +
+    # stats read), then the state is downloaded
     g2 = M.MPM(cs, PREC_MIXED)
     g2.set_surrogate(net)
     ke = args.steps
-    pin = pinned_alloc()
-    ph, ch = M.Particles(p.n, cs.dim, alloc=pin), M.Cells(ncell, cs.dim, alloc=pin)
-    for k in ph.NAMES:
-        getattr(ph, k)[...] = getattr(p, k)
-    for k in ch.NAMES:
-        getattr(ch, k)[...] = getattr(c, k)
-    q = M.Particles(p.n + p.n // 4, cs.dim, alloc=pin)
+    q = M.Particles(ph.cap, cs.dim, alloc=pin)
     cq = M.Cells(ncell, cs.dim, alloc=pin)
-    nbytes = state_bytes(ph, ch)
-    # warm-up of this context (kernel-variant tuning, first-use buffers), then
-    # the timed region starts again from the host state
+    nbytes = state_bytes(ph, ch) * ph.n // max(ph.cap, 1)
+    # warm-up of this context (kernel-variant tuning, first-use buffers)
     g2.upload_particles(ph)
     g2.upload_cells(ch)
+    g2.set_iterate(it_reg)
     g2.advance(args.warmup)
     g2.sync()
     t0 = time.perf_counter()
     g2.upload_particles(ph)
     g2.upload_cells(ch)
-    g2.set_iterate(0)              # the uploaded state is the initial one again
+    g2.set_iterate(it_reg)
     for _ in range(ke):
         g2.advance(1)
         g2.stats()                 # device->host read of dt / max_v / counters
@@ -271,90 +410,88 @@ def run_ours(args):
            "d2h_bytes_per_step": dbytes // ke + 160, "steps": ke, "seconds": te}
     g2.close()
 
-    # ---- plain FP64 GPU path (FMA) on the same case, for the mixed/FP64 ratio ----
+    # ---- plain FP64 GPU path (FMA) from the same regime state ----
     f = M.MPM(cs, PREC_FP64_FMA)
-    f.upload_particles(p)
-    f.upload_cells(c)
+    f.upload_particles(ph)
+    f.upload_cells(ch)
+    f.set_iterate(it_reg)
     f.advance(1)
     kf = max(1, min(2, args.steps))
+    f0 = f.stats()
     msf = f.time_advance(kf)
+    f1 = f.stats()
     fp64 = {"value": ncell * 2 * kf / (msf / 1e3), "ms_per_step": msf / kf, "steps": kf,
-            "speedup_mixed_over_fp64": (ms / args.steps) and (msf / kf) / (ms / args.steps)}
-    # matched-error evidence: both paths after the same number of steps from the same state
-    nsteps_done = args.warmup + args.steps
-    f.advance(nsteps_done - 1 - kf) if nsteps_done - 1 - kf > 0 else None
-    import numpy as np
-    cg, cf = g.download_cells(), f.download_cells()
-    l1 = []
-    for u in range(cs.dim + 2):
-        qg = (cg.alph * cg.coef[:, :, u, 0]).sum(1)
-        qf = (cf.alph * cf.coef[:, :, u, 0]).sum(1)
-        l1.append(float(np.abs(qg - qf).sum() / max(np.abs(qf).sum(), 1e-300)))
-    mom = sum(float(np.abs((cf.alph * cf.coef[:, :, 1 + k, 0]).sum(1)).sum()) for k in range(cs.dim))
-    l1m = [float(np.abs((cg.alph * cg.coef[:, :, 1 + k, 0]).sum(1) - (cf.alph * cf.coef[:, :, 1 + k, 0]).sum(1)).sum()
-                 / max(mom, 1e-300)) for k in range(cs.dim)]
-    fp64["l1_mixed_vs_fp64"] = {"per_variable": l1, "momentum_over_|rho u|": l1m, "steps": nsteps_done}
+            "speedup_mixed_over_fp64": (msf / kf) / (ms / args.steps),
+            "mgfm_iters_per_call": (f1["mgfm_iters"] - f0["mgfm_iters"]) / max(f1["mgfm_calls"] - f0["mgfm_calls"], 1),
+            "state": f"the mixed path's state at t = {regime['t']:.3f} (FP32 values promoted)"}
     f.close()
 
-    # ---- ablation: mixed path with the reference's inline MGFM and plain seed ----
+    # ---- ablation from the same regime state: the reference's inline MGFM and plain seed ----
     a = M.MPM(cs, PREC_MIXED)
-    a.upload_particles(p)
-    a.upload_cells(c)
+    a.upload_particles(ph)
+    a.upload_cells(ch)
+    a.set_iterate(it_reg)
     a.advance(args.warmup)
+    a0 = a.stats()
     msa = a.time_advance(kf)
-    ablation = {"mixed_inline_plain_seed": {"value": ncell * 2 * kf / (msa / 1e3), "ms_per_step": msa / kf,
-                                            "steps": kf}}
+    a1 = a.stats()
+    ablation = {"mixed_inline_plain_seed": {
+        "value": ncell * 2 * kf / (msa / 1e3), "ms_per_step": msa / kf, "steps": kf,
+        "mgfm_iters_per_call": (a1["mgfm_iters"] - a0["mgfm_iters"]) / max(a1["mgfm_calls"] - a0["mgfm_calls"], 1),
+        "learned_over_plain": (msa / kf) / (ms / args.steps)}}
     a.close()
 
     # ---- batched MGFM micro-benchmark (2^24 problems), plain vs learned seed ----
     c5 = None if args.no_c5 else c5_bench(M, S, net)
 
-    # ---- roofline of the dominant kernel ----
-    import math
+    # ---- roofline: the shifting kernel and the whole step against the measured FP32 rate ----
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # the dominant kernel among those with an algorithmic byte count
-    counted = [k for k in prof if k in ("pst", "grid_acc", "g2p", "p2g", "limiter")]
-    dom = max(counted, key=lambda k: prof[k][0]) if counted else None
+    with Clocks(local) as clk_peak:
+        fp32_plain, _ = M.fp32_peak()
+        fp32_packed, _ = M.fp32_peak(packed=True)
+    # the FP32 rate is the larger of the single (FFMA) and packed (FFMA2) loops
+    fp32_tf = max(fp32_plain, fp32_packed)
     roof = None
-    if dom:
-        d_ms, d_cnt = prof[dom]
+    if "pst" in prof:
+        d_ms, d_cnt = prof["pst"]
         per_launch_ms = d_ms / d_cnt
         N = st["n_particles"]
-        # algorithmic bytes per launch (FP32 storage) of the dominant kernel
-        bytes_per = {"pst": N * (2 * 3 * 4 + 2 * 4 + 4 * 4 + 1 + 1 + 3 * 4 + 3 * 4),
-                     "grid_acc": ncell * (2 * 20 * 4 + 2 * 5 * 4 + 2 * 4 + 2 * 20 * 4),
-                     "g2p": N * (3 * 4 * 3 + 4 * 9 + 15 * 4 + 3 * 4 * 2) + ncell * 25 * 4,
-                     "p2g": ncell * (2 * 4 + 2 * 20 * 4) + N * (3 * 4 + 4 + 1),
-                     "limiter": ncell * (2 * 20 * 4 * 1 + 2 * 9 * 4 * 2 + 2 * 5 * 4 + 9 * 4)}.get(dom, 0)
-        achieved = bytes_per / (per_launch_ms / 1e3) / 1e9
-        # FP32 work of the shifting kernel per particle (3D lattice, 8 per cell): 228
-        # candidates x 8 flop (distance test) + 147 members x 33 flop (pair term)
-        flops_per = ({"pst": N * (228 * 8 + 147 * 33), "grid_acc": ncell * 13000}.get(dom, 0)
-                     if cs.dim == 3 else 0)
-        sm_mhz = peaks.get("sm_max_mhz", 2070.0)
-        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-        # DRAM traffic per shifting launch from the ncu capture of the 192x48x48 case
-        # (429.4 MB read + written for 3,538,944 particles), scaled by the particle
-        # count (the traffic grows with it)
-        traffic = 429.4e6 * N / 3538944 if dom == "pst" and CONFIG_ID == 3 else None
-        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic, "traffic_note": "bytes per launch, ncu capture of "
-                "the 192x48x48 case scaled by particles" if traffic else None,
-                "peak_source": "measured" if peaks else "fallback",
+        # algorithmic work per shifting launch (3D lattice, 8 per cell): 228 candidate
+        # tests x 8 flop and 147 members x 33 flop per particle; bytes: positions at
+        # the stage start and end, both smoothing lengths, own density, sound speed,
+        # volume and record, phase, mark_in, v in and tv out (74 B)
+        flops = N * (228 * 8 + 147 * 33) if cs.dim == 3 else N * (50 * 8 + 32 * 33)
+        bytes_per = N * 74
+        achieved = flops / (per_launch_ms / 1e3) / 1e12
+        # DRAM traffic per shifting launch from the ncu capture of the 192x48x48 case,
+        # scaled by the particle count (the traffic grows with it)
+        traffic = PST_TRAFFIC_PER_PARTICLE * N if CONFIG_ID == 3 else None
+        step_flops = 70000.0 * ncell * 2 if cs.dim == 3 else 11000.0 * ncell * 2
+        roof = {"kernel": "pst", "bound": "fp32", "achieved": achieved, "peak": fp32_tf, "unit": "TFLOP/s",
+                "frac": achieved / fp32_tf, "traffic": traffic,
+                "traffic_note": "bytes per launch: ncu capture of the 192x48x48 case scaled by particles"
+                if traffic else None,
+                "peak_source": "measured in this run: pgdg_fp32_peak / pgdg_fp32_peak_packed (independent FFMA "
+                               "and FFMA2 chains on every SM, CUDA events), the larger; clocks "
+                               + json.dumps(clk_peak.summary()),
+                "fp32_measured": {"ffma_tflops": fp32_plain, "ffma2_tflops": fp32_packed},
                 "per_launch_ms": per_launch_ms, "launches": d_cnt,
-                "fp32": ({"achieved_tflops": flops_per / (per_launch_ms / 1e3) / 1e12,
-                          "nominal_peak_tflops": fp32_peak,
-                          "frac": flops_per / (per_launch_ms / 1e3) / 1e12 / fp32_peak}
-                         if flops_per else None)}
+                "hbm": {"achieved": bytes_per / (per_launch_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                        "frac": bytes_per / (per_launch_ms / 1e3) / 1e9 / hbm,
+                        "peak_source": "measured" if peaks else "fallback"},
+                "whole_step": {"achieved": step_flops / (ms / args.steps / 1e3) / 1e12, "peak": fp32_tf,
+                               "unit": "TFLOP/s", "frac": step_flops / (ms / args.steps / 1e3) / 1e12 / fp32_tf,
+                               "work": "70 kflop per 3D cell-stage (11 kflop in 2D)"}}
 
-    cpu = None
+    # ---- accuracy through the interaction on the bounded sample, and the CPU baseline ----
+    accuracy, cpu = None, None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cb = cpu_baseline(steps=1, warmup=1)
+        accuracy, cb = accuracy_sample(M, S, net, SAMPLE_STEPS[CONFIG_ID])
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank == 0:
@@ -362,13 +499,18 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "cells": ncell, "particles": st["n_particles"],
+                           "state": f"advanced untimed to t = {regime['t']:.3f} ({regime['steps']} steps, the "
+                                    f"shock-bubble interaction), then {args.warmup} warm-up steps",
                            "precision": "mixed: FP32 DG residual/limiter/G2P/shifting, FP64 MGFM Newton and P2G "
-                                        "moment sums", "mgfm_seed": "learned (12-64-64-64-2 MLP, BF16 weights and activations on tcgen05 tensor cores) with plain-Newton fallback; interface problems batched per stage",
+                                        "moment sums",
+                           "mgfm_seed": "learned (12-64-64-64-2 MLP, BF16 weights and activations on tcgen05 "
+                                        "tensor cores) with plain-Newton fallback; interface problems batched per stage",
                            "l2": "inputs larger than L2 (state of several GB streamed every step)",
                            "parallelism": f"replicas x{ws}"},
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
-                "cpu_baseline": cpu, "fp64_path": fp64, "ablation": ablation, "mgfm_c5": c5,
-                "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
+                "cpu_baseline": cpu, "fp64_path": fp64, "ablation": ablation, "accuracy": accuracy,
+                "window": window, "regime": regime, "conservation": totals_drift(tot0, tot1),
+                "mgfm_c5": c5, "stage_ms": {k: v[0] / args.steps for k, v in prof.items()},
                 "tuning": {"pst_variant": g.tune("pst")},
                 "stats": {k: st[k] for k in ("n_particles", "n_split", "n_merge", "n_inlet", "n_outlet",
                                              "mgfm_calls", "mgfm_iters", "g2p_fallbacks", "list_entries")}}
@@ -421,6 +563,21 @@ def c5_bench(M, S, net, n=1 << 24, reps=3):
     out["with_root"] = float(conv.mean())
     out["mean_iters_root"] = {k: float(res[k][1][conv].mean()) for k in res}
     out["max_rel_dp"] = float(rel.max())
+    # the tail: both seeds meet |f| <= max(1e-8, 1e-3 |u_l - u_r|), which fixes p*
+    # only within that band where f is flat; its effect on the ghost state the
+    # residual uses (rho*_L and E* = rhoe(p*) + rho* u*^2 / 2 of the left material)
+    gam, pinf = S.C5_GAMMA[mat[conv, 0]], S.C5_PINF[mat[conv, 0]]
+
+    def ghost_e(o):
+        return (o[:, 1] + gam * pinf) / (gam - 1) + 0.5 * o[:, 0] * o[:, 2] ** 2
+    pl, le = res["plain"][0][conv], res["learned"][0][conv]
+    rel_rho = np.abs(le[:, 0] - pl[:, 0]) / np.abs(pl[:, 0])
+    rel_e = np.abs(ghost_e(le) - ghost_e(pl)) / np.abs(ghost_e(pl))
+    out["tail"] = {"problems_rel_dp_above_1e-3": int((rel > 1e-3).sum()),
+                   "fraction_rel_dp_above_1e-3": float((rel > 1e-3).mean()),
+                   "rel_dp_quantiles": {q: float(np.quantile(rel, float(q))) for q in ("0.5", "0.99", "0.999", "0.9999")},
+                   "ghost_rho_max_rel": float(rel_rho.max()), "ghost_rho_rel_q0.999": float(np.quantile(rel_rho, 0.999)),
+                   "ghost_E_max_rel": float(rel_e.max()), "ghost_E_rel_q0.999": float(np.quantile(rel_e, 0.999))}
     out["speedup_learned_over_plain"] = out["plain"]["ms"] / out["learned"]["ms"]
     return out
 
@@ -453,6 +610,9 @@ def main():
                     help="workload: 1 triple point, 2 cylinder, 3 sphere (default, the metric's), 4 underwater "
                          "explosion, 5 the batched MGFM micro-benchmark alone")
     ap.add_argument("--c5-n", type=int, default=1 << 24, help="problems of the batched MGFM micro-benchmark")
+    ap.add_argument("--regime-t", type=float, default=-1.0,
+                    help="simulated time the state is advanced to (untimed) before the timed steps; -1: the "
+                         "workload's default (0.2 for the 3D shock-bubble cases, past the shock-bubble contact)")
     args = ap.parse_args()
     global CONFIG_ID, WORKLOAD, GRID, SAMPLE_GRID
     if args.config == 5:

@@ -188,6 +188,14 @@ int pgdg_profile(pgdg_ctx* ctx, int enable);
 int pgdg_profile_read(pgdg_ctx* ctx, char* names, int names_cap, double* ms, int64_t* counts, int cap, int* n);
 int pgdg_launch_count(pgdg_ctx* ctx, int64_t* n);
 int pgdg_time_advance(pgdg_ctx* ctx, int nsteps, double* ms);
+/* the FP32 fused multiply-add rate of the current device, measured by timing
+ * independent FFMA chains on every SM with CUDA events (the roofline
+ * denominator of the FP32-bound kernels); *ms (may be NULL) receives the
+ * timed launch's duration */
+int pgdg_fp32_peak(double* tflops, double* ms);
+/* the same with the chains as packed pairs (FFMA2, two FP32 multiply-adds per
+ * instruction) */
+int pgdg_fp32_peak_packed(double* tflops, double* ms);
 
 #ifdef __cplusplus
 }

@@ -1448,6 +1448,7 @@ struct OracleT : po_ctx {
 
   /* MPM::MPM_run_simulation (mpm_ini.cpp:682-766) */
   void run_step(int64_t n) override {
+    st.time += dt; /* simulated time (Solver::MPM_Solver's integral_time) */
     if (n == 1) used_state_update();
     bin_particles();
     split_particle_fast();

@@ -754,6 +754,7 @@ struct Ctx : pgdg_ctx {
     s->iterate_num = iterate;
     s->dt = h.dt;
     s->max_v = h.max_v;
+    s->time = h.time;
     return PGDG_OK;
   }
 
@@ -900,6 +901,7 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
   int run_step(int64_t n) override {
+    timed("set_timestep", 1, [&] { Launch<D, R, EX>::add_time(P, st); }); /* simulated time += dt */
     if (n == 1) used_state();
     bin();
     split();

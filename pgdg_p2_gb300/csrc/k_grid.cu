@@ -204,6 +204,15 @@ __global__ void k_dt_final(DevPtrs<R> P) {
   if (!(P.cnt->dt < 1.e19)) atomicOr(&P.cnt->err, ERR_DT);
 }
 
+template <typename R, bool EX>
+__global__ void k_add_time(DevPtrs<R> P) {
+  P.cnt->time += P.cnt->dt;
+}
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::add_time(const DevPtrs<R>& P, cudaStream_t st) {
+  k_add_time<R, EX><<<1, 1, 0, st>>>(P);
+}
+
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::set_timestep(const CaseK& K, const DevPtrs<R>& P, int by_cells, cudaStream_t st) {
   k_dt_init<R, EX><<<1, 1, 0, st>>>(P);
@@ -1232,6 +1241,7 @@ void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out
 #define PGDG_INST(D, R, EX)                                                                     \
   template void Launch<D, R, EX>::used_state(const CaseK&, const DevPtrs<R>&, cudaStream_t);       \
   template void Launch<D, R, EX>::set_timestep(const CaseK&, const DevPtrs<R>&, int, cudaStream_t); \
+  template void Launch<D, R, EX>::add_time(const DevPtrs<R>&, cudaStream_t);                       \
   template void Launch<D, R, EX>::p2g(const CaseK&, const DevPtrs<R>&, bool, cudaStream_t);        \
   template void Launch<D, R, EX>::p2g_new(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \
   template void Launch<D, R, EX>::limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \

@@ -57,6 +57,7 @@ struct DevCounters {
   unsigned int err;
   unsigned int pad;
   double dt, max_v;
+  double time;                    /* simulated time: sum of the steps' dt */
 };
 
 /* case constants handed to kernels by value */
@@ -206,6 +207,7 @@ struct Launch {
   /* k_grid.cu */
   static void used_state(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void set_timestep(const CaseK&, const DevPtrs<R>&, int by_cells, cudaStream_t);
+  static void add_time(const DevPtrs<R>&, cudaStream_t);
   /* fresh_bins: every particle lies in its bucket's cell (right after
    * binning), so neighbour cells beyond the cut radius can be skipped */
   static void p2g(const CaseK&, const DevPtrs<R>&, bool fresh_bins, cudaStream_t);

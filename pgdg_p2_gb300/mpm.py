@@ -62,6 +62,8 @@ def lib():
         L.pgdg_profile_read.argtypes = [vp, C.c_char_p, C.c_int, P(C.c_double), P(C.c_int64), C.c_int, P(C.c_int)]
         L.pgdg_launch_count.argtypes = [vp, P(C.c_int64)]
         L.pgdg_time_advance.argtypes = [vp, C.c_int, P(C.c_double)]
+        L.pgdg_fp32_peak.argtypes = [P(C.c_double), P(C.c_double)]
+        L.pgdg_fp32_peak_packed.argtypes = [P(C.c_double), P(C.c_double)]
         L.pgdg_mgfm_batched.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int64]
         L.pgdg_mgfm_batched_noalloc.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int64]
         L.pgdg_surrogate_create.argtypes = [C.c_int, P(vp)]
@@ -320,3 +322,12 @@ class MPM:
         n = C.c_int64()
         self._ck(lib().pgdg_launch_count(self.h, C.byref(n)), "launch_count")
         return n.value
+
+
+def fp32_peak(packed=False):
+    """Measured FP32 multiply-add rate of the current device (packed: FFMA2
+    pairs): (TFLOP/s, ms of the timed launch)."""
+    tf, ms = C.c_double(), C.c_double()
+    fn = lib().pgdg_fp32_peak_packed if packed else lib().pgdg_fp32_peak
+    check(fn(C.byref(tf), C.byref(ms)), "pgdg_fp32_peak")
+    return tf.value, ms.value

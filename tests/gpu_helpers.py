@@ -37,3 +37,18 @@ def conserved_l1(cs, cg, co):
         if 1 <= u <= cs.dim:
             mom.append(float(np.abs(qg - qo).sum() / max(mag, 1e-300)))
     return per, mom
+
+
+def fp32_perturbed(p, seed=12345):
+    """Particles with every energy scaled by 1 +- 2^-24 (seeded random signs):
+    the size of rounding an FP64 value to FP32."""
+    q = p.copy()
+    sign = np.random.default_rng(seed).choice([-1.0, 1.0], size=q.E.shape)
+    q.E[:] = q.E * (1.0 + sign * 2.0 ** -24)
+    return q
+
+
+def floor_gate(per, floor, tol=1e-3, factor=3.0):
+    """Variables whose relative L1 exceeds max(tol, factor * floor), where floor
+    is the oracle's own L1 under FP32-sized perturbation of its input."""
+    return [(v, e, f) for v, (e, f) in enumerate(zip(per, floor)) if not e <= max(tol, factor * f)]

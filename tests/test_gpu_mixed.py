@@ -1,53 +1,19 @@
 """Mixed-precision path (FP32 residual / limiter / G2P / shifting, FP64 MGFM and
-P2G sums) against the FP64 oracle: relative L1 per conserved variable."""
+P2G sums) against the FP64 oracle: the shifting displacement after one step,
+and the agreement of the shifting kernel's variants."""
 import numpy as np
 import pytest
 
-from tests.gpu_helpers import conserved_l1
-
 pytestmark = pytest.mark.gpu
 
-# tolerance of the accuracy gate: 1e-3 relative L1 per conserved variable
-# (momentum components normalised by the momentum magnitude, because the
-# transverse components are near zero in most of the domain).  Water's
-# stiffened-gas energy is stored shifted by gamma p_inf/(gamma-1) on this path,
-# so the underwater explosion meets the same gate.
-TOL = 1e-3
-
-
-@pytest.mark.parametrize("cid,grid,steps", [(3, (96, 24, 24), 10), (2, (64, 16, 16), 10), (1, (112, 48), 20),
-                                            (4, (128, 128), 10)])
-def test_mixed_l1_vs_oracle(gpu_mod, oracle_mod, cid, grid, steps):
-    M, O = gpu_mod, oracle_mod
-    from pgdg_p2_gb300.abi import PREC_MIXED
-    cs, p, c = M.make_case(cid, grid)
-    g = M.MPM(cs, PREC_MIXED)
-    o = O.Oracle(cs)
-    for x in (g, o):
-        x.upload_particles(p)
-        x.upload_cells(c)
-    for s in range(1, steps + 1):
-        dt, mv = o.Set_timestep()
-        g.Set_timestep()
-        g.set_dt(dt)
-        g.set_max_v(mv)
-        g.set_iterate(s)
-        o.set_iterate(s)
-        g.MPM_run_simulation(s)
-        o.MPM_run_simulation(s)
-    g.sync()
-    per, mom = conserved_l1(cs, g.download_cells(), o.download_cells())
-    assert per[0] <= TOL, per
-    assert per[-1] <= TOL, per
-    assert max(mom) <= TOL, (per, mom)
-    pg, po = g.download_particles(), o.download_particles()
-    assert abs(pg.n - po.n) <= max(2, po.n // 1000)
-
+# the accuracy of whole mixed steps against the oracle, through the
+# shock-bubble interaction, is gated in test_gpu_interaction.py
 
 # particle shifting (particle_flow.cpp:485-622) in the mixed path: the
 # displacement velocity tv - v after one step against the FP64 oracle,
-# relative L1 over the particles present in both (matched by creation rank)
-TOL_SHIFT = 2e-2
+# relative L1 over the particles present in both (matched by creation rank);
+# measured 5e-6 to 1e-4
+TOL_SHIFT = 1e-3
 
 
 @pytest.mark.parametrize("cid,grid", [(3, (96, 24, 24)), (1, (112, 48)), (4, (128, 128))])

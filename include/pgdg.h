@@ -48,6 +48,13 @@ int pgdg_case_cells(const pgdg_case* cs, pgdg_cells* out);
 int pgdg_create(const pgdg_case* cs, int precision, int64_t capacity, pgdg_ctx** out);
 int pgdg_destroy(pgdg_ctx* ctx);
 const char* pgdg_last_error(pgdg_ctx* ctx);
+/* MPM::Initialize_case (mpm_ini.cpp:33-673; fluid particles mpm_ini.cpp:170-294,
+ * cells mpm_ini.cpp:299-346) on the device: workload config_id is built in
+ * place into a context created for the case pgdg_case_setup(config_id, ...)
+ * returned, with no host arrays and no upload.  The state equals
+ * pgdg_case_particles (same seed) and pgdg_case_cells followed by the two
+ * uploads, bit for bit. */
+int pgdg_case_build(pgdg_ctx* ctx, int config_id, uint64_t seed);
 int pgdg_capacity(pgdg_ctx* ctx, int64_t* cap);
 
 /* ---- data movement (host arrays, canonical particle order) ---- */
@@ -88,7 +95,18 @@ int pgdg_run_step(pgdg_ctx* ctx, int64_t n);                       /* MPM::MPM_r
 /* Solver::MPM_Solver (solver.cpp:30-64) without output clipping:
  * nsteps x {Set_timestep, ++iterate_num, MPM_run_simulation}, all on device */
 int pgdg_advance(pgdg_ctx* ctx, int nsteps);
-int pgdg_totals(pgdg_ctx* ctx, double* out6);                      /* conservation totals (Triple_point_2phase/mpm_ini.cpp:599-654) */
+/* conservation totals (Triple_point_2phase/mpm_ini.cpp:599-654): particle mass
+ * per phase, particle energy, cell mass per phase, cell energy; each summed in
+ * double-double and rounded once, so the result does not depend on the order
+ * of the addends */
+int pgdg_totals(pgdg_ctx* ctx, double* out6);
+/* MPM::Output_point (mpm_ini.cpp:774-824) on the device: out5 = the largest and
+ * smallest x of the phase-2 particles near the axis (y, z < 2.5 p_sz: the
+ * bubble's downstream end and the jet), the smallest x of those away from it
+ * (y or z > 4 p_sz: the upstream end), the phase-2 mass sum rho vol, and the
+ * number of fluid particles (the rows of pointa.txt and mass.txt); the ends
+ * start at the box's left and right x */
+int pgdg_output_point(pgdg_ctx* ctx, double* out5);
 
 /* ---- MGFM seed surrogate (new; the reference starts Newton from max(p_l,p_r),
  *      mpm.cpp:893) ----
@@ -160,10 +178,13 @@ int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8
 /* ---- CUDA graphs of whole steps (no reference counterpart) ----
  * pgdg_advance replays captured graphs of three steps (one per rotation of
  * the coordinate buffers) when a step reads nothing back on the host: not at
- * the first iteration, not while per-method timing or the interface queue is
- * on, not before the shifting kernel's variant is tuned.  Results equal the
- * eager steps bit for bit.  on = 0 runs every step eagerly.  Uploads and
- * changes of surrogate, queue or kernel variant drop the graphs. */
+ * the first iteration, not while per-method timing is on, not before the
+ * shifting kernel's variant is tuned.  With the interface queue (and the seed
+ * surrogate) the stage's problem count stays on the device and sizes the
+ * batch there; between calls the host grows the queue when a stage passed half
+ * of it, and a stage that outgrows it is solved inline.  Results equal the
+ * eager steps bit for bit.  on = 0 runs every step eagerly.  Uploads, queue
+ * growth and changes of surrogate, queue or kernel variant drop the graphs. */
 int pgdg_set_graphs(pgdg_ctx* ctx, int on);
 
 /* ---- kernel variants (no reference counterpart) ----
@@ -175,7 +196,9 @@ int pgdg_set_graphs(pgdg_ctx* ctx, int on);
  * kernel "p2g_skip": 1 (default) lets pgdg_mls_p2g skip neighbour cells beyond
  * its cut radius while every particle still lies in its bucket's cell (from
  * pgdg_bin_particles until particles move); 0 always visits all 3^d cells.
- * Both give identical sums. */
+ * Both give identical sums.  "iface_cap": variant >= 0 fixes the interface
+ * queue's capacity at that many problems (a stage beyond it is solved inline;
+ * a memory bound for large cases), -1 returns to automatic growth. */
 int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen);
 
 /* ---- measurement ----

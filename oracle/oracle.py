@@ -51,6 +51,7 @@ def lib():
         L.po_run_step.argtypes = [vp, C.c_int64]
         L.po_advance.argtypes = [vp, C.c_int]
         L.po_totals.argtypes = [vp, P(C.c_double)]
+        L.po_output_point.argtypes = [vp, P(C.c_double)]
         L.po_set_threads.argtypes = [C.c_int]
         L.po_mgfm_batched.argtypes = [P(C.c_double), P(C.c_int8), P(C.c_double), P(C.c_double), C.c_int,
                                       P(C.c_double), P(C.c_double), P(C.c_int32), C.c_int64]
@@ -214,6 +215,11 @@ class Oracle:
 
     def advance(self, nsteps):
         lib().po_advance(self.h, int(nsteps))
+
+    def output_point(self):
+        out = np.zeros(5)
+        lib().po_output_point(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
 
     def totals(self):
         out = np.zeros(6)

@@ -58,6 +58,7 @@ struct po_ctx {
   virtual void update_particle(int md) = 0;
   virtual void run_step(int64_t n) = 0;
   virtual void totals(double* out) = 0;
+  virtual void output_point(double* out) = 0;
   double dt = 0, max_v = 1e-7;
   int64_t iterate = 0;
   pgdg_stats st{};
@@ -1464,20 +1465,56 @@ struct OracleT : po_ctx {
     }
   }
 
+  /* double-double running sum (TwoSum of each addend, the errors summed beside
+   * it: Neumaier's compensated summation), rounded once: the result does not
+   * depend on the order of the addends (the reference reduces under TBB in no
+   * fixed order) */
+  struct DDs {
+    double hi = 0, lo = 0;
+    void add(double b) {
+      const double s = hi + b, bb = s - hi;
+      lo += (hi - (s - bb)) + (b - bb);
+      hi = s;
+    }
+    double value() const { return hi + lo; }
+  };
+  /* conservation totals (Triple_point_2phase/mpm_ini.cpp:599-654: particle
+   * mass per phase and energy, cell mass per phase and energy) */
   void totals(double* out) override {
-    double pm[F] = {0, 0}, pe = 0, cm[F] = {0, 0}, ce = 0;
+    DDs pm[F], pe, cm[F], ce;
     for (int p : fluid) {
-      pm[phase[p] - 1] += rho[p] * vol[p];
-      pe += E[p] * vol[p];
+      pm[phase[p] - 1].add(rho[p] * vol[p]);
+      pe.add(E[p] * vol[p]);
     }
     double voli = cs.p_size[0] * cs.p_size[1] * (D == 3 ? cs.p_size[2] : 1.0);
     for (int64_t ci : used_list)
       for (int s = 0; s < F; s++) {
         if (cph[ci * F + s] != 1) continue;
-        cm[s] += voli * calph[ci * F + s] * crho[ci * F + s];
-        ce += voli * calph[ci * F + s] * cE[ci * F + s];
+        cm[s].add(voli * calph[ci * F + s] * crho[ci * F + s]);
+        ce.add(voli * calph[ci * F + s] * cE[ci * F + s]);
       }
-    out[0] = pm[0]; out[1] = pm[1]; out[2] = pe; out[3] = cm[0]; out[4] = cm[1]; out[5] = ce;
+    out[0] = pm[0].value(); out[1] = pm[1].value(); out[2] = pe.value();
+    out[3] = cm[0].value(); out[4] = cm[1].value(); out[5] = ce.value();
+  }
+  /* MPM::Output_point (mpm_ini.cpp:774-824): bubble extents along the axis and
+   * the phase-2 mass, over particle_fluid in order (the ends start at the
+   * box's left and right x) */
+  void output_point(double* out) override {
+    double dw = cs.box_l[0], jet = cs.box_r[0], ups = cs.box_r[0];
+    DDs mass;
+    const double a = 2.5 * cs.p_sz, b = 4 * cs.p_sz;
+    for (int p : fluid) {
+      if (phase[p] != 2) continue;
+      const double px = x[3 * p], py = x[3 * p + 1], pz = D == 3 ? x[3 * p + 2] : 0.0;
+      if (py < a && pz < a) {
+        if (px > dw) dw = px;
+        if (px < jet) jet = px;
+      } else if (py > b || pz > b) {
+        if (px < ups) ups = px;
+      }
+      mass.add(rho[p] * vol[p]);
+    }
+    out[0] = dw; out[1] = jet; out[2] = ups; out[3] = mass.value(); out[4] = (double)fluid.size();
   }
 
   /* ------------------------------------------------------------------ */
@@ -1693,6 +1730,10 @@ int po_get_stats(po_ctx* ctx, pgdg_stats* st) {
   return PGDG_OK;
 }
 int po_set_timestep(po_ctx* ctx, double* dt, double* mv) { return ctx->set_timestep(dt, mv); }
+int po_output_point(po_ctx* ctx, double* out5) {
+  ctx->output_point(out5);
+  return PGDG_OK;
+}
 int po_used_state_update(po_ctx* ctx) { ctx->used_state_update(); return PGDG_OK; }
 int po_bin_particles(po_ctx* ctx) { ctx->bin_particles(); return PGDG_OK; }
 int po_split_particle_fast(po_ctx* ctx) { ctx->split_particle_fast(); return PGDG_OK; }

@@ -66,6 +66,7 @@ int po_run_step(po_ctx* ctx, int64_t n);     /* MPM_run_simulation */
 /* Solver::MPM_Solver without output clipping: set_timestep, ++iterate, run_step */
 int po_advance(po_ctx* ctx, int nsteps);
 int po_totals(po_ctx* ctx, double* out);     /* [F particle mass, particle E, F cell mass, cell E] */
+int po_output_point(po_ctx* ctx, double* out5); /* Output_point: bubble extents, phase-2 mass, count */
 
 /* batched MGFM with an explicit material table (gamma[m], pinf[m]) */
 int po_mgfm_batched(const double* in6, const int8_t* mat2, const double* gam, const double* pinf,

@@ -28,6 +28,7 @@ CU = [("k_particles.cu", "k_particles", ["-fmad=false"]),
       ("k_xfer.cu", "k_xfer", []),
       ("k_mlp_tc.cu", "k_mlp_tc", []),
       ("k_peak.cu", "k_peak", []),
+      ("k_case.cu", "k_case", ["-fmad=false"]),
       ("capi.cu", "capi", [])]
 CPP = ["case_builder.cpp"]
 

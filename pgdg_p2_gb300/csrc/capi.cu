@@ -30,7 +30,8 @@ struct pgdg_ctx {
   int iface_queue = 0;   /* 1: interface problems solved as one batch */
   int pst_var = -1;      /* shifting-kernel variant (-1: tune at the next call) */
   int p2g_skip = 1;      /* 1: P2G skips out-of-reach neighbour cells while the bins are fresh */
-  int64_t iface_last = 0;
+  int64_t iface_cap_fixed = -1; /* >= 0: the interface queue's capacity, never grown */
+  virtual int set_iface_cap(int64_t cap) = 0;
   virtual int iface_download(double*, int8_t*, int64_t, int64_t*) = 0;
   /* captured step graphs (advance): dropped when what they bake in changes */
   virtual void invalidate_graphs() = 0;
@@ -38,6 +39,8 @@ struct pgdg_ctx {
   int64_t iterate = 0;
   cudaStream_t st = nullptr;
   virtual int upload_particles(const pgdg_particles*) = 0;
+  virtual int output_point(double* out5) = 0;
+  virtual int case_build(int id, uint64_t seed) = 0;
   virtual int download_particles(pgdg_particles*) = 0;
   virtual int num_particles(int64_t*) = 0;
   virtual int upload_cells(const pgdg_cells*) = 0;
@@ -62,6 +65,7 @@ struct pgdg_ctx {
   virtual int update_grid(int) = 0;
   virtual int update_particle(int) = 0;
   virtual int run_step(int64_t) = 0;
+  virtual int prepare_step() = 0; /* host-side upkeep between steps */
   virtual int advance(int) = 0;
   virtual int totals(double*) = 0;
   virtual int check() = 0;
@@ -239,7 +243,7 @@ struct Ctx : pgdg_ctx {
     P.qcap = (int64_t)nc;
     if (const size_t rsb = Launch<D, R, EX>::pst_scratch_bytes(K)) CK(A(&pst_scratch, rsb));
     CK(A(&P.cnt, 1));
-    CK(A(&d_tot, 6));
+    CK(A(&d_tot, Launch<D, R, EX>::totals_scratch()));
     /* interface queue: at most 2 phases x 2D faces x 4 points x 1 other phase per cell;
      * sized for a few per cent of the cells, grown on demand */
     Q.cap = std::max<int64_t>(1 << 16, K.ncell / 8);
@@ -248,6 +252,7 @@ struct Ctx : pgdg_ctx {
     CK(A(&Q.out3, 3 * (size_t)Q.cap));
     CK(A(&Q.off, nc + 1));
     CK(A(&Q.blk, (nc + 2047) / 2048 + 2));
+    CK(A(&Q.tot, 2));
     CK(A(&d_ncell, 1));
     {
       unsigned long long v = (unsigned long long)K.ncell;
@@ -399,6 +404,38 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
   static int scan_nblk_host(int64_t cap) { return (int)((cap + 2047) / 2048); }
+
+  /* the case's particles and cells built on the device, in place of
+   * pgdg_case_particles / pgdg_case_cells and the two uploads */
+  int case_build(int id, uint64_t seed) override {
+    drop_graphs();
+    fresh_bins = false;
+    const int64_t n = pgdg_case_num_particles(&cs);
+    if (n > K.cap) {
+      err = "particle count exceeds capacity";
+      return PGDG_EINVAL;
+    }
+    CK(cudaStreamSynchronize(st));
+    P.xb = 0;
+    P.hb = 0;
+    x0b = 0;
+    CK(cudaMemsetAsync(P.phase, 0, (size_t)K.cap, st));
+    const int rc = pgdg::case_build<D, R>(K, P, cs, id, seed, n, st);
+    if (rc) {
+      err = "case_build: the case does not match the workload";
+      return rc;
+    }
+    CK(cudaStreamSynchronize(st));
+    DevCounters hc = counters();
+    hc.n_slots = n;
+    hc.n_live = n;
+    hc.seq_next = (unsigned long long)n;
+    hc.arena_used = 0;
+    hc.err = 0;
+    hc.n_dirty = hc.n_flagged = 0;
+    CK(cudaMemcpy(P.cnt, &hc, sizeof(hc), cudaMemcpyHostToDevice));
+    return PGDG_OK;
+  }
 
   /* ---------------- exchange ---------------- */
   int upload_particles(const pgdg_particles* pp) override {
@@ -803,8 +840,10 @@ struct Ctx : pgdg_ctx {
   int iface_download(double* in6, int8_t* mat2, int64_t cap, int64_t* n) override {
     flush_prof();
     CK(cudaStreamSynchronize(st));
-    *n = iface_last;
-    const int64_t m = std::min<int64_t>(cap, iface_last);
+    unsigned long long t[2] = {0, 0};
+    if (iface_queue && !EX) CK(cudaMemcpy(t, Q.tot, sizeof(t), cudaMemcpyDeviceToHost));
+    *n = (int64_t)t[1];
+    const int64_t m = std::min<int64_t>(cap, (int64_t)t[1]);
     if (m > 0) {
       CK(cudaMemcpy(in6, Q.in6, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(mat2, Q.mat, 2 * m, cudaMemcpyDeviceToHost));
@@ -837,15 +876,43 @@ struct Ctx : pgdg_ctx {
     return bv;
   }
   int grow_queue(int64_t need) {
+    drop_graphs(); /* they hold the old buffers */
+    CK(cudaStreamSynchronize(st));
     for (void* p : {(void*)Q.in6, (void*)Q.mat, (void*)Q.out3}) {
       for (auto& a : allocs)
         if (a == p) a = nullptr;
       cudaFree(p);
     }
-    Q.cap = need + need / 2;
+    Q.cap = need;
     CK(A(&Q.in6, 6 * (size_t)Q.cap));
     CK(A(&Q.mat, 2 * (size_t)Q.cap));
     CK(A(&Q.out3, 3 * (size_t)Q.cap));
+    return PGDG_OK;
+  }
+  /* Host-side upkeep of the interface queue, between steps: grow it to twice
+   * the last stage's problem count when that passed half its capacity, and
+   * hold the batch scratch for its capacity, so that steps (captured or not)
+   * never allocate or read back.  A stage that still outgrows the queue is
+   * solved inline by the residual. */
+  int ensure_queue() {
+    if (!iface_queue || EX) return PGDG_OK;
+    unsigned long long t[2] = {0, 0};
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(t, Q.tot, sizeof(t), cudaMemcpyDeviceToHost));
+    if (iface_cap_fixed < 0 && (int64_t)t[0] * 2 > Q.cap) {
+      int rc = grow_queue((int64_t)t[0] * 2 + 4096);
+      if (rc) return rc;
+    }
+    const int rc = mgfm_seeded_reserve(net, part, Q.cap);
+    if (rc) err = "interface batch scratch: out of device memory";
+    return rc;
+  }
+  bool capturing = false;
+  int prepare_step() override { return ensure_queue(); }
+  int set_iface_cap(int64_t cap) override {
+    iface_cap_fixed = cap;
+    if (cap >= 0 && cap != Q.cap) return grow_queue(cap > 0 ? cap : 1);
+    drop_graphs();
     return PGDG_OK;
   }
   int grid_acc() override {
@@ -854,22 +921,20 @@ struct Ctx : pgdg_ctx {
       return PGDG_OK;
     }
     /* surrogate-seeded MGFM: queue the interface problems, solve them in one
-     * batch, then evaluate the residual with the queued ghost states */
-    int64_t n = 0;
-    timed("iface_gather", 6, [&] { n = Launch<D, R, EX>::iface_gather(K, P, Q, st); });
-    if (n < 0) {
-      int rc = grow_queue(-n);
+     * batch, then evaluate the residual with the queued ghost states.  The
+     * batch's size stays on the device (Q.tot): nothing is read back */
+    if (!capturing) {
+      const int rc = mgfm_seeded_reserve(net, part, Q.cap);
       if (rc) return rc;
-      timed("iface_gather", 6, [&] { n = Launch<D, R, EX>::iface_gather(K, P, Q, st); });
     }
-    iface_last = n;
+    timed("iface_gather", 6, [&] { Launch<D, R, EX>::iface_gather(K, P, Q, st); });
     int rc = PGDG_OK;
-    timed("mgfm_seeded", 3, [&] {
-      rc = mgfm_seeded_run(net, Q.in6, Q.mat, d_gam, d_pinf, K.mgfm_variant, Q.out3, nullptr, n, &P.cnt->mgfm_calls,
-                           part, st);
+    timed("mgfm_seeded", net ? 8 : 6, [&] {
+      rc = mgfm_seeded_run(net, Q.in6, Q.mat, d_gam, d_pinf, K.mgfm_variant, Q.out3, nullptr, Q.cap,
+                           &P.cnt->mgfm_calls, part, st, Q.tot + 1);
     });
     if (rc) return rc;
-    timed("grid_acc", 1, [&] { Launch<D, R, EX>::grid_acc_queued(K, P, Q, st); });
+    timed("grid_acc", 2, [&] { Launch<D, R, EX>::grid_acc_queued(K, P, Q, st); });
     return PGDG_OK;
   }
   int update_grid(int md) override {
@@ -922,12 +987,13 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
   /* ---------------- CUDA graphs of whole steps ----------------
-   * A step without the interface queue reads nothing back on the host, so
-   * advance() captures it.  The coordinate buffers rotate with a period of three
-   * steps (the buffer indices are kernel arguments), so the graph holds three
-   * steps, one per rotation phase P.xb.  Steps that cannot be captured run
-   * eagerly: the first iteration (Used_state_update, the particle-based CFL
-   * step), any step while per-method timing or the queue is on, a step before
+   * A step reads nothing back on the host (the interface queue is sized on
+   * the device and checked by ensure_queue() between calls), so advance()
+   * captures it.  The coordinate buffers rotate with a period of three steps
+   * (the buffer indices are kernel arguments), so the graph holds three steps,
+   * one per rotation phase P.xb.  Steps that cannot be captured run eagerly:
+   * the first two iterations (Used_state_update, and Set_timestep's rule while
+   * iterate_num <= 1), any step while per-method timing is on, a step before
    * the kernel-variant tuning, and the remainder of a call below three steps. */
   struct StepGraph {
     cudaGraphExec_t exec = nullptr;
@@ -952,11 +1018,13 @@ struct Ctx : pgdg_ctx {
     const int64_t it0 = iterate, l0 = launches;
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PGDG_ECUDA;
+    capturing = true;
     for (int k = 0; k < 3; k++) {
       set_timestep(nullptr, nullptr);
       iterate++;
       run_step(iterate);
     }
+    capturing = false;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     sg.xb_after = P.xb;
     sg.hb_after = P.hb;
@@ -981,9 +1049,11 @@ struct Ctx : pgdg_ctx {
     return PGDG_OK;
   }
   int advance(int nsteps) override {
+    int rc = ensure_queue();
+    if (rc) return rc;
     int s = 0;
     while (s < nsteps) {
-      const bool graphable = graphs_enabled && !prof && !iface_queue && iterate >= 1 && pst_var >= 0 && nsteps - s >= 3;
+      const bool graphable = graphs_enabled && !prof && iterate >= 2 && pst_var >= 0 && nsteps - s >= 3;
       if (graphable) {
         StepGraph& sg = graphs[P.xb];
         if (!sg.exec && capture3(sg) != PGDG_OK) {
@@ -1007,6 +1077,13 @@ struct Ctx : pgdg_ctx {
       run_step(iterate);
       s++;
     }
+    return PGDG_OK;
+  }
+  /* Output_point (mpm_ini.cpp:774-824) on the device; 5 doubles come back */
+  int output_point(double* out5) override {
+    Launch<D, R, EX>::probe(K, P, d_tot, d_tot, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(out5, d_tot, 5 * sizeof(double), cudaMemcpyDeviceToHost));
     return PGDG_OK;
   }
   int totals(double* out) override {
@@ -1070,6 +1147,14 @@ int pgdg_destroy(pgdg_ctx* ctx) {
 const char* pgdg_last_error(pgdg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 int pgdg_capacity(pgdg_ctx* ctx, int64_t* cap) { return ctx->capacity(cap); }
 int pgdg_upload_particles(pgdg_ctx* ctx, const pgdg_particles* p) { return ctx->upload_particles(p); }
+int pgdg_output_point(pgdg_ctx* ctx, double* out5) {
+  if (!ctx || !out5) return PGDG_EINVAL;
+  return ctx->output_point(out5);
+}
+int pgdg_case_build(pgdg_ctx* ctx, int config_id, uint64_t seed) {
+  if (!ctx || config_id < 1 || config_id > 4) return PGDG_EINVAL;
+  return ctx->case_build(config_id, seed);
+}
 int pgdg_download_particles(pgdg_ctx* ctx, pgdg_particles* p) { return ctx->download_particles(p); }
 int pgdg_num_particles(pgdg_ctx* ctx, int64_t* n) { return ctx->num_particles(n); }
 int pgdg_upload_cells(pgdg_ctx* ctx, const pgdg_cells* c) { return ctx->upload_cells(c); }
@@ -1103,6 +1188,11 @@ int pgdg_set_graphs(pgdg_ctx* ctx, int on) {
   return PGDG_OK;
 }
 int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen) {
+  if (kernel && std::strcmp(kernel, "iface_cap") == 0 && variant >= -1) {
+    const int rc = ctx->set_iface_cap(variant);
+    if (chosen) *chosen = variant;
+    return rc;
+  }
   if (kernel && std::strcmp(kernel, "p2g_skip") == 0 && variant >= -2 && variant <= 1) {
     if (variant >= 0) ctx->p2g_skip = variant;
     if (variant >= 0) ctx->invalidate_graphs();
@@ -1110,7 +1200,7 @@ int pgdg_tune(pgdg_ctx* ctx, const char* kernel, int variant, int* chosen) {
     return PGDG_OK;
   }
   if (!kernel || std::strcmp(kernel, "pst") != 0 || variant < -2) {
-    ctx->err = "tunable kernels: pst (variant >= -2), p2g_skip (0, 1, or -2 to query)";
+    ctx->err = "tunable kernels: pst (variant >= -2), p2g_skip (0, 1, or -2 to query), iface_cap (>= -1)";
     return PGDG_EINVAL;
   }
   if (variant >= 0) ctx->pst_var = variant;
@@ -1149,7 +1239,10 @@ int pgdg_calculate_limiter(pgdg_ctx* ctx) { return ctx->limiter(); }
 int pgdg_grid_acceleration(pgdg_ctx* ctx) { return ctx->grid_acc(); }
 int pgdg_update_grid(pgdg_ctx* ctx, int md) { return ctx->update_grid(md); }
 int pgdg_update_particle(pgdg_ctx* ctx, int md) { return ctx->update_particle(md); }
-int pgdg_run_step(pgdg_ctx* ctx, int64_t n) { return ctx->run_step(n); }
+int pgdg_run_step(pgdg_ctx* ctx, int64_t n) {
+  const int rc = ctx->prepare_step();
+  return rc ? rc : ctx->run_step(n);
+}
 int pgdg_advance(pgdg_ctx* ctx, int nsteps) { return ctx->advance(nsteps); }
 int pgdg_totals(pgdg_ctx* ctx, double* out6) { return ctx->totals(out6); }
 

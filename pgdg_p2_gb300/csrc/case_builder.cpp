@@ -17,6 +17,8 @@
 #include <cmath>
 #include <cstring>
 
+#include "case_math.h"
+
 namespace {
 
 constexpr double PI_REF = 3.1415926;
@@ -27,55 +29,10 @@ inline double powern(double a, int n) {
   return r;
 }
 
-/* splitmix64 */
-inline uint64_t splitmix64(uint64_t& s) {
-  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-inline double u01(uint64_t& s) { return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
+using namespace pgdg_case_math;
 
-/* Mach-1.22 shock into air at rest (gamma 1.4, rho 1, p 1): Rankine-Hugoniot */
 void post_shock(double& rho2, double& u2, double& p2) {
-  const double g = 1.4, M = 1.22, r1 = 1.0, p1 = 1.0;
-  double M2 = M * M;
-  p2 = p1 * (1.0 + 2.0 * g / (g + 1.0) * (M2 - 1.0));
-  rho2 = r1 * (g + 1.0) * M2 / ((g - 1.0) * M2 + 2.0);
-  double c1 = std::sqrt(g * p1 / r1);
-  u2 = M * c1 * (1.0 - r1 / rho2);
-}
-
-struct Region { int phase; double rho, p, u[3]; };
-
-Region region_of(int id, const double* x) {
-  Region r{1, 1.0, 1.0, {0, 0, 0}};
-  switch (id) {
-    case 1:
-      if (x[0] < 1.0) r = {1, 1.0, 1.0, {0, 0, 0}};
-      else if (x[1] < 1.5) r = {1, 1.0, 0.1, {0, 0, 0}};
-      else r = {2, 0.125, 0.1, {0, 0, 0}};
-      break;
-    case 2:
-    case 3: {
-      double rho2, u2, p2;
-      post_shock(rho2, u2, p2);
-      double d2 = (x[0] - 1.5) * (x[0] - 1.5) + x[1] * x[1];
-      if (id == 3) d2 += x[2] * x[2];
-      if (x[0] < 1.0) r = {1, rho2, p2, {u2, 0, 0}};
-      else if (d2 < 0.25 * 0.25) r = {2, 0.138, 1.0, {0, 0, 0}};
-      else r = {1, 1.0, 1.0, {0, 0, 0}};
-      break;
-    }
-    case 4: {
-      double d2 = x[0] * x[0] + x[1] * x[1];
-      if (d2 < 0.3 * 0.3) r = {2, 1270.0, 8.29e8, {0, 0, 0}};
-      else r = {1, 1000.0, 1e5, {0, 0, 0}};
-      break;
-    }
-    default: break;
-  }
-  return r;
+  pgdg_case_math::post_shock(rho2, u2, p2, std::sqrt(1.4 * 1.0 / 1.0));
 }
 
 int npart_axis(const pgdg_case* cs, int d) {
@@ -164,41 +121,34 @@ int pgdg_case_particles(const pgdg_case* cs, int id, uint64_t seed, pgdg_particl
   const int U = D + 2;
   const int NS = U * D;
   int na[3] = {npart_axis(cs, 0), npart_axis(cs, 1), npart_axis(cs, 2)};
-  uint64_t rs = seed ? seed : 20260101ull;
+  const uint64_t rs = seed ? seed : 20260101ull;
   const double jit = (id == 1) ? cs->p_g / 8.0 : 0.0;
   double vol0 = powern(cs->p_sz, D);
   double h0 = 3.2 / 2. * cs->p_sz;
+  double ps[3];
+  post_shock(ps[0], ps[1], ps[2]);
   int64_t p = 0;
   for (int i = 0; i < na[0]; i++)
     for (int j = 0; j < na[1]; j++)
       for (int k = 0; k < na[2]; k++, p++) {
-        double x[3] = {cs->box_l[0] + (i + 0.5) * cs->p_sz, cs->box_l[1] + (j + 0.5) * cs->p_sz, 0.0};
-        if (D == 3) x[2] = cs->box_l[2] + (k + 0.5) * cs->p_sz;
-        if (jit > 0)
-          for (int d = 0; d < D; d++) x[d] += (2.0 * u01(rs) - 1.0) * jit;
-        Region r = region_of(id, x);
-        int s = r.phase - 1;
-        double g = cs->gamma[s], pinf = cs->pinf[s];
+        const PState0 s = lattice_particle(id, D, cs->box_l, cs->p_sz, jit, rs, p, i, j, k, vol0, h0, cs->gamma,
+                                           cs->pinf, ps);
         for (int d = 0; d < 3; d++) {
-          out->coord[3 * p + d] = x[d];
-          if (out->v) out->v[3 * p + d] = (d < D) ? r.u[d] : 0.0;
+          out->coord[3 * p + d] = s.x[d];
+          if (out->v) out->v[3 * p + d] = s.u[d];
           if (out->tv) out->tv[3 * p + d] = 0.0;
-          out->rhov[3 * p + d] = (d < D) ? r.u[d] * r.rho : 0.0;
+          out->rhov[3 * p + d] = s.rhov[d];
         }
-        out->vol[p] = vol0;
-        out->mass[p] = vol0 * r.rho;
-        out->h[p] = h0;
-        out->P[p] = r.p;
-        out->rho[p] = r.rho;
-        double vv = 0;
-        for (int d = 0; d < D; d++) vv += r.u[d] * r.u[d];
-        double E = (r.p + g * pinf) / (g - 1);
-        E += 0.5 * r.rho * vv;
-        out->E[p] = E;
-        out->c[p] = std::sqrt(g * (r.p + pinf) / r.rho);
+        out->vol[p] = s.vol;
+        out->mass[p] = s.mass;
+        out->h[p] = s.h;
+        out->P[p] = s.P;
+        out->rho[p] = s.rho;
+        out->E[p] = s.E;
+        out->c[p] = s.c;
         if (out->slope)
           for (int t = 0; t < NS; t++) out->slope[NS * p + t] = 0.0;
-        out->phase[p] = r.phase;
+        out->phase[p] = s.phase;
         if (out->mark_in) out->mark_in[p] = 0;
         if (out->seq) out->seq[p] = (uint64_t)p;
       }

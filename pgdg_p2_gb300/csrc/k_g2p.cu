@@ -516,6 +516,7 @@ constexpr int SCAN_RED = 66;
 template <typename R>
 struct RowSortBufs {
   typename Vec4<R>::T *run, *row;
+  typename Vec4<R>::T* rec; /* each sorted entry's G2P record (new position, signed volume) */
   uint16_t* rk;            /* cell offset in the row of each sorted entry */
   int32_t *off, *pmin, *pmax;
   RowKey<R> *kmin, *kmax, *pmaxk, *smink;
@@ -523,6 +524,7 @@ struct RowSortBufs {
 template <typename R>
 struct RowSorted {
   const typename Vec4<R>::T* row;
+  const typename Vec4<R>::T* rec; /* the entries' G2P records, in the same order */
   const uint16_t* rk;
   const int32_t* pmin;  /* per cell: rank of its first and last entry in its row */
   const int32_t* pmax;
@@ -540,6 +542,7 @@ __host__ __device__ inline size_t rowsort_layout(const CaseK& K, unsigned char* 
   };
   unsigned char* run = take(ne * sizeof(V4));
   unsigned char* row = take(ne * sizeof(V4));
+  unsigned char* rec = take(ne * sizeof(V4));
   unsigned char* rk = take(ne * sizeof(uint16_t));
   unsigned char* off = take(nc * sizeof(int32_t));
   unsigned char* pmn = take(nc * sizeof(int32_t));
@@ -551,6 +554,7 @@ __host__ __device__ inline size_t rowsort_layout(const CaseK& K, unsigned char* 
   if (B) {
     B->run = reinterpret_cast<V4*>(run);
     B->row = reinterpret_cast<V4*>(row);
+    B->rec = reinterpret_cast<V4*>(rec);
     B->rk = reinterpret_cast<uint16_t*>(rk);
     B->off = reinterpret_cast<int32_t*>(off);
     B->pmin = reinterpret_cast<int32_t*>(pmn);
@@ -739,6 +743,7 @@ __global__ void __launch_bounds__(256) k_rs_rank(CaseK K, DevPtrs<R> P, RowSortB
           if (j != k) rank += rs_count_less<D, R>(K, P, B, rw * NR + j, key);
       }
       B.row[RB + rank] = v;
+      B.rec[RB + rank] = reinterpret_cast<const V4*>(P.rec)[slot_of<R>(v.w)];
       B.rk[RB + rank] = (uint16_t)k;
       if (r == 0) B.pmin[c] = rank;
       if (r == cnt - 1) B.pmax[c] = rank;
@@ -785,6 +790,58 @@ __device__ __forceinline__ int block_scan_counts(int* a, int n, int* s_red) {
   const int total = s_red[64];
   __syncthreads();
   return total;
+}
+
+/* Bound_pen and Update_PST of one particle from its neighbour sums */
+template <int D, typename R, bool EX>
+__device__ __forceinline__ void pst_finish(const CaseK& K, const DevPtrs<R>& P, int64_t p, R dt,
+                                           const PstPart<D, R, EX>& pp) {
+  /* Bound_pen (particle_flow.cpp:587-622) on the faces of the particle's cell */
+  R bp[3] = {0, 0, 0};
+  {
+    const int64_t ci = P.lcell[p];
+    int idx[3];
+    idx[2] = (int)(ci % K.N[2]);
+    idx[1] = (int)((ci / K.N[2]) % K.N[1]);
+    idx[0] = (int)(ci / ((int64_t)K.N[1] * K.N[2]));
+#pragma unroll
+    for (int f = 0; f < 2 * D; f++) {
+      const int a = (f == 0 || f == 2) ? 1 : (f == 1 || f == 3) ? 0 : 2;
+      const int sg = (f == 0 || f == 3 || f == 4) ? -1 : 1;
+      const int side = (f == 0) ? 2 : (f == 1) ? 1 : (f == 2) ? 3 : (f == 3) ? 0 : (f == 4) ? 4 : 5;
+      int nbi = idx[a] + sg;
+      if (nbi >= 0 && nbi < K.N[a]) continue;
+      if (K.bc[side] == 0) continue;
+      R cen = (R)(K.bl[a] + K.ps[a] * (idx[a] + 0.5) + sg * 0.5 * K.ps[a]);
+      R nn = (R)sg;
+      R ds = (pp.xnp[a] - cen) * nn;
+      if (ds < R(0)) nn = -nn;
+      R dis = fabs(ds);
+      if (dis < R(0.4) * (R)K.p_sz) bp[a] += R(0.02) / dis * (pp.c_p * pp.c_p) * nn;
+    }
+  }
+  /* Update_PST (particle_flow.cpp:485-525) */
+  const R px = (R)K.p_sz;
+  R dx[3], dx1[3], dx2[3];
+  R s0 = 0, s1 = 0, s2 = 0;
+  for (int d = 0; d < D; d++) {
+    dx[d] = pp.pst[d] * dt * dt / R(2.);
+    dx1[d] = pp.phs[d] * dt * dt / R(2.);
+    dx2[d] = bp[d] * dt * dt / R(2.);
+    s0 = (d == 0) ? dx[d] * dx[d] : s0 + dx[d] * dx[d];
+    s1 = (d == 0) ? dx1[d] * dx1[d] : s1 + dx1[d] * dx1[d];
+    s2 = (d == 0) ? dx2[d] * dx2[d] : s2 + dx2[d] * dx2[d];
+  }
+  R dis0 = sqrt_r<R>(s0), dis1 = sqrt_r<R>(s1), dis2 = sqrt_r<R>(s2);
+  R l0 = amin1(px / R(10), dis0) / (dis0 + R(1e-20));
+  R l1 = amin1(px / R(10), dis1) / (dis1 + R(1e-20));
+  R l2 = amin1(px / R(2), dis2) / (dis2 + R(1e-20));
+  const bool mk = P.mark_in[p] == 1;
+  for (int d = 0; d < D; d++) {
+    R dv = (dx[d] * l0 + dx1[d] * l1 + dx2[d] * l2) / dt;
+    if (mk) dv = R(0);
+    P.tv[d * K.cap + p] = P.v[d * K.cap + p] + dv;
+  }
 }
 
 /* one particle: neighbour sum, Bound_pen, Update_PST; sm == nullptr -> global path */
@@ -1056,52 +1113,7 @@ __device__ void pst_particle(const CaseK& K, const DevPtrs<R>& P, int64_t p, con
           }
         }
   }
-  /* Bound_pen (particle_flow.cpp:587-622) on the faces of the particle's cell */
-  R bp[3] = {0, 0, 0};
-  {
-    const int64_t ci = P.lcell[p];
-    int idx[3];
-    idx[2] = (int)(ci % K.N[2]);
-    idx[1] = (int)((ci / K.N[2]) % K.N[1]);
-    idx[0] = (int)(ci / ((int64_t)K.N[1] * K.N[2]));
-#pragma unroll
-    for (int f = 0; f < 2 * D; f++) {
-      const int a = (f == 0 || f == 2) ? 1 : (f == 1 || f == 3) ? 0 : 2;
-      const int sg = (f == 0 || f == 3 || f == 4) ? -1 : 1;
-      const int side = (f == 0) ? 2 : (f == 1) ? 1 : (f == 2) ? 3 : (f == 3) ? 0 : (f == 4) ? 4 : 5;
-      int nbi = idx[a] + sg;
-      if (nbi >= 0 && nbi < K.N[a]) continue;
-      if (K.bc[side] == 0) continue;
-      R cen = (R)(K.bl[a] + K.ps[a] * (idx[a] + 0.5) + sg * 0.5 * K.ps[a]);
-      R nn = (R)sg;
-      R ds = (pp.xnp[a] - cen) * nn;
-      if (ds < R(0)) nn = -nn;
-      R dis = fabs(ds);
-      if (dis < R(0.4) * (R)K.p_sz) bp[a] += R(0.02) / dis * (pp.c_p * pp.c_p) * nn;
-    }
-  }
-  /* Update_PST (particle_flow.cpp:485-525) */
-  const R px = (R)K.p_sz;
-  R dx[3], dx1[3], dx2[3];
-  R s0 = 0, s1 = 0, s2 = 0;
-  for (int d = 0; d < D; d++) {
-    dx[d] = pp.pst[d] * dt * dt / R(2.);
-    dx1[d] = pp.phs[d] * dt * dt / R(2.);
-    dx2[d] = bp[d] * dt * dt / R(2.);
-    s0 = (d == 0) ? dx[d] * dx[d] : s0 + dx[d] * dx[d];
-    s1 = (d == 0) ? dx1[d] * dx1[d] : s1 + dx1[d] * dx1[d];
-    s2 = (d == 0) ? dx2[d] * dx2[d] : s2 + dx2[d] * dx2[d];
-  }
-  R dis0 = sqrt_r<R>(s0), dis1 = sqrt_r<R>(s1), dis2 = sqrt_r<R>(s2);
-  R l0 = amin1(px / R(10), dis0) / (dis0 + R(1e-20));
-  R l1 = amin1(px / R(10), dis1) / (dis1 + R(1e-20));
-  R l2 = amin1(px / R(2), dis2) / (dis2 + R(1e-20));
-  const bool mk = P.mark_in[p] == 1;
-  for (int d = 0; d < D; d++) {
-    R dv = (dx[d] * l0 + dx1[d] * l1 + dx2[d] * l2) / dt;
-    if (mk) dv = R(0);
-    P.tv[d * K.cap + p] = P.v[d * K.cap + p] + dv;
-  }
+  pst_finish<D, R, EX>(K, P, p, dt, pp);
 }
 
 template <int D, typename R, bool EX, int VAR>
@@ -1322,16 +1334,393 @@ static void pst_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int 
   k_pst<D, R, EX, VAR><<<nbx * nb1 * nb0, pst_threads(VAR), bytes, st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap, RS);
 }
 
+/* ---- the shifting kernel, second form (variants 6 and 7) ----
+ * The same bricks, row-sorted staging and chord search as the direct variants,
+ * with three changes:
+ *   - members' G2P records are read in row order: the row sort places each
+ *     entry's record beside it (variant 6 reads them from there through L1,
+ *     variant 7 stages them in shared memory too: one block per SM with room
+ *     for 12 particles per cell);
+ *   - a brick whose cells hold more particles than its staging room (the
+ *     compressed fluid behind a shock) scans the same sorted rows from global
+ *     memory instead of falling back to the per-cell scan;
+ *   - on the FP32 path, candidates are tested and their pair terms evaluated
+ *     two at a time with packed arithmetic (FADD2/FMUL2/FFMA2: one instruction
+ *     for both); a non-member's term is masked to zero, which keeps the lanes
+ *     of a warp in step.
+ * The members, each term's arithmetic and the order of the sum are those of
+ * the direct variants. */
+template <int D, typename R, bool SREC, bool GL>
+__device__ __forceinline__ void pst2_rows(const CaseK& K, const DevPtrs<R>& P, const RowSorted<R>& RS,
+                                          const int* s_off, const long long* s_rsrc, const R* s_rlo,
+                                          const R* s_rhi, const typename Vec4<R>::T* s_ent,
+                                          const typename Vec4<R>::T* s_rec, const unsigned char* s_tag,
+                                          const int* slo, const int* sn, const int* lo, const int* hi,
+                                          PstPart<D, R, false>& pp) {
+  using V4 = typename Vec4<R>::T;
+  constexpr int RA = D - 1;
+  const int clo = lo[RA] - slo[RA], chi = hi[RA] - slo[RA];
+  const R zp = pp.xsp[RA];
+  const R lim2m = pp.lim2 * R(1.0001);
+  const int u1 = (D == 3) ? hi[1] : lo[1];
+  for (int t = lo[0]; t <= hi[0]; t++)
+    for (int u = lo[1]; u <= u1; u++) {
+      const int row = (D == 3) ? (t - slo[0]) * sn[1] + (u - slo[1]) : (t - slo[0]);
+      R dxy = R(0);
+      for (int d = 0; d < D - 1; d++) {
+        R a = s_rlo[2 * row + d] - pp.xsp[d], b = pp.xsp[d] - s_rhi[2 * row + d];
+        R w = a > b ? a : b;
+        if (w > R(0)) dxy += w * w;
+      }
+      if (!(dxy <= lim2m)) continue;
+      const R hw = sqrt_r<R>(lim2m - dxy); /* half chord of the 2h sphere */
+      const R za = zp - hw, zb = zp + hw;
+      const int eb = s_off[row], ee = s_off[row + 1];
+      const long long dl = s_rsrc[row] - eb;
+      auto ENT = [&](int e) -> V4 { return GL ? RS.row[e + dl] : s_ent[e]; };
+      auto REC = [&](int e) -> V4 { return (SREC && !GL) ? s_rec[e] : RS.rec[e + dl]; };
+      auto TAG = [&](int e) -> int {
+        if constexpr (GL) return (int)RS.rk[e + dl] - slo[RA];
+        else return (int)s_tag[e];
+      };
+      auto ZOF = [&](const V4& v) -> R { return RA == 2 ? v.z : v.y; };
+      int e = eb, hi_e = ee;
+      while (e < hi_e) { /* first entry with coordinate >= za */
+        const int m = (e + hi_e) >> 1;
+        if (ZOF(ENT(m)) < za) e = m + 1;
+        else hi_e = m;
+      }
+      for (; e < ee; e += 2) {
+        const bool hasb = e + 1 < ee;
+        const V4 va = ENT(e), vb = ENT(hasb ? e + 1 : e);
+        if (ZOF(va) > zb) break;
+        const bool inb = hasb && !(ZOF(vb) > zb);
+        const int ta = TAG(e), tb = TAG(hasb ? e + 1 : e);
+        bool ma = (unsigned)(ta - clo) <= (unsigned)(chi - clo);
+        bool mb = inb && (unsigned)(tb - clo) <= (unsigned)(chi - clo);
+        /* within 2h at the stage start (the direct variants' test, both entries at once) */
+        R ddA, ddB;
+        if constexpr (sizeof(R) == 4) {
+          float2 dx = __fadd2_rn(make_float2(pp.xsp[0], pp.xsp[0]), make_float2(-va.x, -vb.x));
+          float2 dd = __fmul2_rn(dx, dx);
+          float2 dy = __fadd2_rn(make_float2(pp.xsp[1], pp.xsp[1]), make_float2(-va.y, -vb.y));
+          dd = __ffma2_rn(dy, dy, dd);
+          if constexpr (D == 3) {
+            float2 dz = __fadd2_rn(make_float2(pp.xsp[2], pp.xsp[2]), make_float2(-va.z, -vb.z));
+            dd = __ffma2_rn(dz, dz, dd);
+          }
+          ddA = dd.x;
+          ddB = dd.y;
+        } else {
+          R xa[3] = {va.x, va.y, va.z}, xb[3] = {vb.x, vb.y, vb.z};
+          ddA = ddB = R(0);
+          for (int d = 0; d < D; d++) {
+            R t0 = pp.xsp[d] - xa[d], t1 = pp.xsp[d] - xb[d];
+            ddA = (d == 0) ? t0 * t0 : ddA + t0 * t0;
+            ddB = (d == 0) ? t1 * t1 : ddB + t1 * t1;
+          }
+        }
+        ma = ma && ddA <= pp.lim2;
+        mb = mb && ddB <= pp.lim2;
+        if (ma || mb) {
+          const V4 ra = REC(e), rb = REC(hasb ? e + 1 : e);
+          if constexpr (sizeof(R) == 4) {
+            const float2 drx = __fadd2_rn(make_float2(pp.xnp[0], pp.xnp[0]), make_float2(-ra.x, -rb.x));
+            const float2 dry = __fadd2_rn(make_float2(pp.xnp[1], pp.xnp[1]), make_float2(-ra.y, -rb.y));
+            float2 drz = make_float2(0.f, 0.f);
+            float2 d2 = __fmul2_rn(drx, drx);
+            d2 = __ffma2_rn(dry, dry, d2);
+            if constexpr (D == 3) {
+              drz = __fadd2_rn(make_float2(pp.xnp[2], pp.xnp[2]), make_float2(-ra.z, -rb.z));
+              d2 = __ffma2_rn(drz, drz, d2);
+            }
+            /* a coincident pair contributes nothing (the reference skips it) */
+            const bool ka = ma && d2.x > 0.f, kb = mb && d2.y > 0.f;
+            const float2 rq = make_float2(ka ? rsqrtf(d2.x) : 0.f, kb ? rsqrtf(d2.y) : 0.f);
+            float2 sv = __fmul2_rn(__fmul2_rn(d2, rq), make_float2(pp.inv_hh, pp.inv_hh));
+            /* beyond the support (s >= 2) W and its gradient vanish: q = 0 there */
+            sv.x = fminf(sv.x, 2.f);
+            sv.y = fminf(sv.y, 2.f);
+            const float2 q = __ffma2_rn(sv, make_float2(-0.5f, -0.5f), make_float2(1.f, 1.f));
+            const float2 q2 = __fmul2_rn(q, q), q3 = __fmul2_rn(q2, q);
+            /* the direct variants' arithmetic, operation for operation:
+             * w = q^4 (1 + 2s), rr = cwr w, tmp1 = tmp1c + tmp1c5 rr^4,
+             * f = aw_c q^3 tmp1 vol */
+            const float2 w = __fmul2_rn(__fmul2_rn(q2, q2), __ffma2_rn(sv, make_float2(2.f, 2.f), make_float2(1.f, 1.f)));
+            const float2 rr = __fmul2_rn(make_float2(pp.cwr, pp.cwr), w);
+            const float2 rr2 = __fmul2_rn(rr, rr);
+            const float2 t1 = __ffma2_rn(make_float2(pp.tmp1c5, pp.tmp1c5), __fmul2_rn(rr2, rr2),
+                                         make_float2(pp.tmp1c, pp.tmp1c));
+            const float2 vm = make_float2(ka ? fabsf(ra.w) : 0.f, kb ? fabsf(rb.w) : 0.f);
+            const float2 f = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(pp.aw_c, pp.aw_c), q3), t1), vm);
+            /* summed in candidate order, as the direct variants do */
+            if (ka) {
+              pp.pst[0] = fmaf(drx.x, f.x, pp.pst[0]);
+              pp.pst[1] = fmaf(dry.x, f.x, pp.pst[1]);
+              if constexpr (D == 3) pp.pst[2] = fmaf(drz.x, f.x, pp.pst[2]);
+            }
+            if (kb) {
+              pp.pst[0] = fmaf(drx.y, f.y, pp.pst[0]);
+              pp.pst[1] = fmaf(dry.y, f.y, pp.pst[1]);
+              if constexpr (D == 3) pp.pst[2] = fmaf(drz.y, f.y, pp.pst[2]);
+            }
+            /* across the interface: the sharpening term (rare) */
+            const bool xa = ka && rec_phase(ra.w) != pp.ph, xb = kb && rec_phase(rb.w) != pp.ph;
+            if (xa || xb) {
+              for (int k = 0; k < 2; k++) {
+                if (!(k == 0 ? xa : xb)) continue;
+                const int32_t qs = slot_of<R>(k == 0 ? va.w : vb.w);
+                const R* rc2 = P.rec2 + 2 * (int64_t)qs;
+                const R rhoq = rc2[0], cq = rc2[1];
+                const R tmp2 = R(1.) / (pp.rho_p + rhoq);
+                const R cs = R(-0.1) * tmp2 * (pp.crho_p + cq * cq * rhoq);
+                const R g = cs * pp.aw_c * (k == 0 ? q3.x : q3.y) * (k == 0 ? vm.x : vm.y);
+                pp.phs[0] += (k == 0 ? drx.x : drx.y) * g;
+                pp.phs[1] += (k == 0 ? dry.x : dry.y) * g;
+                if constexpr (D == 3) pp.phs[2] += (k == 0 ? drz.x : drz.y) * g;
+              }
+            }
+          } else {
+            if (ma) {
+              R xnq[3] = {ra.x, ra.y, ra.z};
+              pp.add(xnq, fabs(ra.w), rec_phase(ra.w), P.rec2 + 2 * (int64_t)slot_of<R>(va.w), nullptr);
+            }
+            if (mb) {
+              R xnq[3] = {rb.x, rb.y, rb.z};
+              pp.add(xnq, fabs(rb.w), rec_phase(rb.w), P.rec2 + 2 * (int64_t)slot_of<R>(vb.w), nullptr);
+            }
+          }
+        }
+        if (!inb) break;
+      }
+    }
+}
+
+template <int D, typename R, bool SREC>
+__global__ void __launch_bounds__(512, SREC ? 1 : 2) k_pst2(CaseK K, DevPtrs<R> P, int xs, int hs, int xn, int hn,
+                                                            int nb0, int nb1, int cap, RowSorted<R> RS) {
+  using BK = BigBrick<D>;
+  using V4 = typename Vec4<R>::T;
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  const R dt = (R)P.cnt->dt;
+  const R max_v = (R)P.cnt->max_v;
+  const R* XS = P.X[xs];
+  const R* XN = P.X[xn];
+  const R* HS = P.H[hs];
+  const R* HN = P.H[hn];
+  const int b = blockIdx.x;
+  int c0[3];
+  c0[0] = (b / (nb0 * nb1)) * BK::B0;
+  c0[1] = ((b / nb0) % nb1) * BK::B1;
+  c0[2] = (D == 3) ? (b % nb0) * BK::B2 : 0;
+  const int bdim[3] = {BK::B0, BK::B1, D == 3 ? BK::B2 : 1};
+  int slo[3], sn[3];
+  for (int d = 0; d < 3; d++) {
+    const int r = (d < D) ? K.rad2 : 0;
+    const int Nd = (d < D) ? K.N[d] : 1;
+    slo[d] = max(c0[d] - r, 0);
+    sn[d] = min(c0[d] + bdim[d] - 1 + r, Nd - 1) - slo[d] + 1;
+  }
+  const int nsc = sn[0] * sn[1] * sn[2];
+  const int nrow = (D == 3) ? sn[0] * sn[1] : sn[0];
+  constexpr int RA = D - 1;
+  /* shared layout: off[nrow+1] | rsrc[nrow] | rlo[2 nrow] | rhi[2 nrow] | bnd[nsc] | ent[cap] | rec[cap] | tag[cap] */
+  size_t o = 0;
+  auto take = [&](size_t bytes, size_t al) {
+    o = (o + al - 1) / al * al;
+    const size_t r0 = o;
+    o += bytes;
+    return smem_raw + r0;
+  };
+  int* s_off = reinterpret_cast<int*>(take(sizeof(int) * (nrow + 1), 16));
+  long long* s_rsrc = reinterpret_cast<long long*>(take(sizeof(long long) * nrow, 16));
+  R* s_rlo = reinterpret_cast<R*>(take(sizeof(R) * 2 * nrow, 16));
+  R* s_rhi = reinterpret_cast<R*>(take(sizeof(R) * 2 * nrow, 16));
+  int* s_bnd = reinterpret_cast<int*>(take(sizeof(int) * nsc, 16));
+  V4* s_ent = reinterpret_cast<V4*>(take(sizeof(V4) * cap, 32));
+  V4* s_rec = SREC ? reinterpret_cast<V4*>(take(sizeof(V4) * cap, 32)) : nullptr;
+  unsigned char* s_tag = take(cap, 16);
+  __shared__ int s_red[SCAN_RED];
+  for (int l = threadIdx.x; l < nsc; l += blockDim.x) {
+    const int t = l / (sn[1] * sn[2]), s = (l / sn[2]) % sn[1], m = l % sn[2];
+    const int64_t c = ((int64_t)(slo[0] + t) * K.N[1] + (slo[1] + s)) * K.N[2] + (slo[2] + m);
+    s_bnd[l] = P.boff[c + 1] > P.boff[c] ? 1 : 0;
+  }
+  const int NR = K.N[RA];
+  for (int row = threadIdx.x; row < nrow; row += blockDim.x) {
+    const int64_t gr = (D == 3) ? (int64_t)(slo[0] + row / sn[1]) * K.N[1] + (slo[1] + row % sn[1])
+                                : (int64_t)(slo[0] + row);
+    int first = INT_MAX, last = -1;
+    for (int k = 0; k < sn[RA]; k++) {
+      const int64_t c = gr * NR + slo[RA] + k;
+      first = min(first, RS.pmin[c]);
+      last = max(last, RS.pmax[c]);
+    }
+    s_off[row + 1] = last >= first ? last - first + 1 : 0;
+    s_rsrc[row] = gr * NR * K.maxpc + (last >= first ? first : 0);
+  }
+  __syncthreads();
+  const int s_total = block_scan_counts(s_off, nrow, s_red);
+  const bool use_sm = s_total <= cap;
+  /* one warp per row: the row's bounds in the other axes (always), and the
+   * copy of its range with each entry's window tag (when it fits) */
+  {
+    const int lane = threadIdx.x & 31;
+    for (int row = threadIdx.x >> 5; row < nrow; row += blockDim.x >> 5) {
+      const int e0 = s_off[row], len = s_off[row + 1] - e0;
+      const int64_t src = s_rsrc[row];
+      R mn[2] = {R(1e30), R(1e30)}, mx[2] = {R(-1e30), R(-1e30)};
+      for (int i = lane; i < len; i += 32) {
+        const V4 v = RS.row[src + i];
+        if (use_sm) {
+          const int kk = (int)RS.rk[src + i] - slo[RA];
+          s_ent[e0 + i] = v;
+          s_tag[e0 + i] = (unsigned char)((kk >= 0 && kk < sn[RA]) ? kk : 255);
+          if constexpr (SREC) s_rec[e0 + i] = RS.rec[src + i];
+        }
+        const R xv[2] = {v.x, v.y};
+        for (int d = 0; d < D - 1; d++) {
+          mn[d] = xv[d] < mn[d] ? xv[d] : mn[d];
+          mx[d] = xv[d] > mx[d] ? xv[d] : mx[d];
+        }
+      }
+      for (int d = 0; d < D - 1; d++) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const R a = __shfl_xor_sync(0xffffffffu, mn[d], off), bb = __shfl_xor_sync(0xffffffffu, mx[d], off);
+          mn[d] = a < mn[d] ? a : mn[d];
+          mx[d] = bb > mx[d] ? bb : mx[d];
+        }
+      }
+      if (lane < D - 1) {
+        s_rlo[2 * row + lane] = lane == 0 ? mn[0] : mn[1];
+        s_rhi[2 * row + lane] = lane == 0 ? mx[0] : mx[1];
+      }
+    }
+  }
+  __syncthreads();
+  /* the brick's own particles, one per thread */
+  const int nbc = bdim[0] * bdim[1] * bdim[2];
+  __shared__ int s_boff[BK::B0 * BK::B1 * BK::B2 + 1];
+  __shared__ int s_bcell[BK::B0 * BK::B1 * BK::B2];
+  for (int q = threadIdx.x; q < nbc; q += blockDim.x) {
+    const int d0 = q / (bdim[1] * bdim[2]), d1 = (q / bdim[2]) % bdim[1], d2 = q % bdim[2];
+    const int ci = c0[0] + d0, cj = c0[1] + d1, ck = c0[2] + d2;
+    int cnt = 0;
+    int64_t c = -1;
+    if (ci < K.N[0] && cj < K.N[1] && ck < K.N[2]) {
+      c = ((int64_t)ci * K.N[1] + cj) * K.N[2] + ck;
+      cnt = min(P.bcnt[c], K.maxpc);
+    }
+    s_bcell[q] = (int)c;
+    s_boff[q + 1] = cnt;
+  }
+  __syncthreads();
+  const int npart = block_scan_counts(s_boff, nbc, s_red);
+  for (int i = threadIdx.x; i < npart; i += blockDim.x) {
+    int q = 0, qh = nbc - 1;
+    while (q < qh) {
+      const int md = (q + qh + 1) >> 1;
+      if (s_boff[md] <= i) q = md;
+      else qh = md - 1;
+    }
+    const int64_t c = s_bcell[q];
+    const int32_t p = P.bucket[c * K.maxpc + (i - s_boff[q])];
+    PstPart<D, R, false> pp;
+    pp.ph = P.phase[p];
+    for (int d = 0; d < 3; d++) pp.xsp[d] = pp.xnp[d] = R(0);
+    for (int d = 0; d < D; d++) {
+      pp.xsp[d] = XS[d * K.cap + p];
+      pp.xnp[d] = XN[d * K.cap + p];
+    }
+    pp.hs_p = HS[p];
+    pp.hh = HN[p];
+    pp.rho_p = P.rho[p];
+    pp.c_p = P.c[p];
+    pp.init(K, max_v);
+    int pos[3], lo[3], hi[3];
+    cell_pos<D, R>(K, pp.xsp, pos);
+    bool inside = true;
+    for (int d = 0; d < 3; d++) {
+      const int r = (d < D) ? K.rad2 : 0;
+      lo[d] = max(pos[d] - r, 0);
+      hi[d] = min(pos[d] + r, (d < D ? K.N[d] : 1) - 1);
+      if (lo[d] < slo[d] || hi[d] >= slo[d] + sn[d]) inside = false;
+    }
+    if (!inside) {
+      /* drifted out of the staged box: the per-cell scan in the reference's order */
+      pst_particle<D, R, false, 0>(K, P, p, XS, XN, HS, HN, dt, max_v, nullptr);
+      continue;
+    }
+    if (use_sm)
+      pst2_rows<D, R, SREC, false>(K, P, RS, s_off, s_rsrc, s_rlo, s_rhi, s_ent, s_rec, s_tag, slo, sn, lo, hi, pp);
+    else
+      pst2_rows<D, R, SREC, true>(K, P, RS, s_off, s_rsrc, s_rlo, s_rhi, s_ent, s_rec, s_tag, slo, sn, lo, hi, pp);
+    bool edge = false;
+    for (int d = 0; d < D; d++) edge = edge || lo[d] == 0 || hi[d] == K.N[d] - 1;
+    if (edge)
+      for (int t = lo[0]; t <= hi[0]; t++)
+        for (int s = lo[1]; s <= hi[1]; s++)
+          for (int m = lo[2]; m <= hi[2]; m++) {
+            const int l = ((t - slo[0]) * sn[1] + (s - slo[1])) * sn[2] + (m - slo[2]);
+            if (!s_bnd[l]) continue;
+            const int64_t cc = ((int64_t)t * K.N[1] + s) * K.N[2] + m;
+            pst_boundary_cell<D, R, false>(K, P, cc, pp);
+          }
+    pst_finish<D, R, false>(K, P, p, dt, pp);
+  }
+}
+
+template <int D, typename R, bool SREC>
+static void pst2_launch(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, int xn, int hn, const RowSorted<R>& RS,
+                        cudaStream_t st) {
+  using BK = BigBrick<D>;
+  using V4 = typename Vec4<R>::T;
+  const int nb0 = (D == 3) ? (K.N[2] + BK::B2 - 1) / BK::B2 : 1;
+  const int nb1 = (K.N[1] + BK::B1 - 1) / BK::B1;
+  const int nbx = (K.N[0] + BK::B0 - 1) / BK::B0;
+  const int r = K.rad2;
+  const int nsc = (BK::B0 + 2 * r) * (BK::B1 + 2 * r) * (D == 3 ? BK::B2 + 2 * r : 1);
+  const int nrow = (D == 3) ? (BK::B0 + 2 * r) * (BK::B1 + 2 * r) : (BK::B0 + 2 * r);
+  const int ppc = (D == 3) ? 8 : 4;
+  /* staging room per staged cell: 9 particles (variant 6: two blocks per SM),
+   * 12 (variant 7: the fluid compressed behind a shock still fits) */
+  int cap = SREC ? nsc * ppc * 3 / 2 : nsc * ppc * 9 / 8;
+  auto bytes_for = [&](int cp) {
+    size_t o = 0;
+    auto take = [&](size_t bb, size_t al) { o = (o + al - 1) / al * al + bb; };
+    take(sizeof(int) * (nrow + 1), 16);
+    take(sizeof(long long) * nrow, 16);
+    take(sizeof(R) * 2 * nrow, 16);
+    take(sizeof(R) * 2 * nrow, 16);
+    take(sizeof(int) * nsc, 16);
+    take(sizeof(V4) * cp, 32);
+    if (SREC) take(sizeof(V4) * cp, 32);
+    take(cp, 16);
+    return o + 64;
+  };
+  const size_t limit = SREC ? 210 * 1024 : 100 * 1024;
+  while (bytes_for(cap) > limit && cap > 256) cap = cap * 7 / 8;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_pst2<D, R, SREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr_set = true;
+  }
+  k_pst2<D, R, SREC><<<nbx * nb1 * nb0, 512, bytes_for(cap), st>>>(K, P, xs, hs, xn, hn, nb0, nb1, cap, RS);
+}
+
 /* variants of the shifting kernel (the same members; results equal to rounding,
  * since variant 1 sums boundary particles in a second pass; the context's
  * autotuner times them on its own state and keeps the fastest): 0 per-lane row scan with
  * queued members, 1 warp-cooperative row scan, 2 per-lane scan summing members
  * at once, 3 the same for 3 blocks per SM, 4 direct sums over bricks of twice
  * the cells with 512 threads, 5 over bricks of four times the cells with 1024
- * threads.  The exact path has one. */
+ * threads, 6 and 7 the second form (row-ordered records, global-row scan of
+ * over-full bricks, packed pair arithmetic; 7 stages the records too).  The
+ * exact path has one. */
 template <int D, typename R, bool EX>
 int Launch<D, R, EX>::pst_variants() {
-  return EX ? 1 : 6;
+  return EX ? 1 : 8;
 }
 
 /* device scratch of the per-stage row sort (0 on the exact path) */
@@ -1370,12 +1759,14 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
   } else {
     RowSortBufs<R> B;
     rowsort_layout<R>(K, static_cast<unsigned char*>(scratch), &B);
-    const RowSorted<R> RS{B.row, B.rk, B.pmin, B.pmax};
+    const RowSorted<R> RS{B.row, B.rec, B.rk, B.pmin, B.pmax};
     if (var == 1) pst_launch<D, R, EX, 1>(K, P, xs, hs, xn, hn, RS, st);
     else if (var == 2) pst_launch<D, R, EX, 2>(K, P, xs, hs, xn, hn, RS, st);
     else if (var == 3) pst_launch<D, R, EX, 3>(K, P, xs, hs, xn, hn, RS, st);
     else if (var == 4) pst_launch<D, R, EX, 5>(K, P, xs, hs, xn, hn, RS, st);
     else if (var == 5) pst_launch<D, R, EX, 6>(K, P, xs, hs, xn, hn, RS, st);
+    else if (var == 6) pst2_launch<D, R, false>(K, P, xs, hs, xn, hn, RS, st);
+    else if (var == 7) pst2_launch<D, R, true>(K, P, xs, hs, xn, hn, RS, st);
     else pst_launch<D, R, EX, 0>(K, P, xs, hs, xn, hn, RS, st);
   }
 }

@@ -629,8 +629,26 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(6)) k_limiter(CaseK K, D
           R dU = R(0);
           for (int b = 0; b < D; b++) dU = (b == 0) ? co[u][1 + b] * dr[b] : dU + co[u][1 + b] * dr[b];
           R sd = R(1);
-          if (dU >= R(0)) sd = limiter_fn<R>(fabs(qdiv<R, EX>(u_max[s][u], dU + R(1e-20))), lim_fg);
-          else if (dU < R(0)) sd = limiter_fn<R>(fabs(qdiv<R, EX>(u_min[s][u], dU + R(1e-20))), lim_fg);
+          if constexpr (EX) {
+            if (dU >= R(0)) sd = limiter_fn<R>(fabs(qdiv<R, EX>(u_max[s][u], dU + R(1e-20))), lim_fg);
+            else if (dU < R(0)) sd = limiter_fn<R>(fabs(qdiv<R, EX>(u_min[s][u], dU + R(1e-20))), lim_fg);
+          } else if (dU == dU) {
+            /* The ratio |u / (dU + 1e-20)|.  A negative dU equal to -1e-20 in
+             * the working precision makes the denominator zero, which is far
+             * likelier in FP32 (a slope of 1e-20 / dr turns up at symmetry
+             * planes) and gives inf or NaN, and the boundary limiter form
+             * (|ds| + ds) / (|ds| + 1) of inf is NaN.  Here a zero numerator
+             * gives 0 (its value for any non-zero denominator) and the ratio is
+             * capped at 1e30, where the limiter is 1 (interior) or 2 (boundary)
+             * as for every ratio above about 1e8, and the minimum with lim <= 1
+             * ignores it either way: the result equals the reference's wherever
+             * the reference's is finite. */
+            const R um = dU >= R(0) ? u_max[s][u] : u_min[s][u];
+            R ds = fabs(qdiv<R, EX>(um, dU + R(1e-20)));
+            if (um == R(0)) ds = R(0);
+            else if (!(ds <= R(1e30))) ds = R(1e30);
+            sd = limiter_fn<R>(ds, lim_fg);
+          }
           lim[s][u] = amin1(lim[s][u], sd);
         }
       }
@@ -710,6 +728,12 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(MODE == 0 ? 2 : 3)) k_gr
   const R inv[4] = {R(1. / (voli_d + 1e-20)), R(1. / (mij1 + 1e-20)), R(1. / (mij2 + 1e-20)),
                     R(1. / (mij3 + 1e-20))};
   unsigned long long ncall = 0, nit = 0, nmax = 0;
+  /* with the interface queue, a stage whose problems outgrew it runs the inline
+   * solve (MODE 0 launched beside MODE 3): exactly one of the two does work */
+  if (Q.tot) {
+    const bool over = Q.tot[0] > (unsigned long long)Q.cap;
+    if ((MODE == 3 && over) || (MODE == 0 && !over)) return;
+  }
   GRID_STRIDE(ci, nc) {
     if (!P.cused[ci]) continue;
     int idx[3];
@@ -1060,8 +1084,12 @@ __global__ void k_iface_count(CaseK K, DevPtrs<R> P, unsigned long long* cnt) {
   }
 }
 template <typename R, bool EX>
-__global__ void k_iface_total(const unsigned long long* blk, int nblk, unsigned long long* off, int64_t nc) {
-  off[nc] = blk[nblk];
+__global__ void k_iface_total(const unsigned long long* blk, int nblk, unsigned long long* off, int64_t nc,
+                              unsigned long long* tot, int64_t cap) {
+  const unsigned long long n = blk[nblk];
+  off[nc] = n;
+  tot[0] = n;
+  tot[1] = n <= (unsigned long long)cap ? n : 0ull; /* an overflowing stage batches nothing */
 }
 
 template <int D, typename R, bool EX>
@@ -1074,20 +1102,18 @@ void Launch<D, R, EX>::grid_acc(const CaseK& K, const DevPtrs<R>& P, cudaStream_
   k_grid_acc<D, R, EX, 0><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, m1, m2, m3, Q);
 }
 
+/* count, offsets and gather of the stage's interface problems, all on the
+ * device: the count is never read back; a stage with more problems than the
+ * queue holds batches none of them and the residual solves it inline */
 template <int D, typename R, bool EX>
-int64_t Launch<D, R, EX>::iface_gather(const CaseK& K, const DevPtrs<R>& P, IfaceQ Q, cudaStream_t st) {
+void Launch<D, R, EX>::iface_gather(const CaseK& K, const DevPtrs<R>& P, IfaceQ Q, cudaStream_t st) {
   double voli = K.ps[0] * K.ps[1];
   if (D == 3) voli = voli * K.ps[2];
   k_iface_count<D, R, EX><<<grid_for(K.ncell, BLK), BLK, 0, st>>>(K, P, Q.off);
   scan_u64(Q.off, Q.blk, Q.d_ncell, K.ncell, st);
   const int nblk = (int)((K.ncell + 2047) / 2048);
-  k_iface_total<R, EX><<<1, 1, 0, st>>>(Q.blk, nblk, Q.off, K.ncell);
-  unsigned long long tot = 0;
-  cudaMemcpyAsync(&tot, Q.off + K.ncell, sizeof(tot), cudaMemcpyDeviceToHost, st);
-  cudaStreamSynchronize(st);
-  if ((int64_t)tot > Q.cap) return -(int64_t)tot;
+  k_iface_total<R, EX><<<1, 1, 0, st>>>(Q.blk, nblk, Q.off, K.ncell, Q.tot, Q.cap);
   k_grid_acc<D, R, EX, 2><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, 0, 0, 0, Q);
-  return (int64_t)tot;
 }
 
 template <int D, typename R, bool EX>
@@ -1097,6 +1123,8 @@ void Launch<D, R, EX>::grid_acc_queued(const CaseK& K, const DevPtrs<R>& P, Ifac
   double ps[3] = {K.ps[0] / 2, K.ps[1] / 2, K.ps[2] / 2};
   double m1 = (ps[0] * ps[0] / 3.) * voli, m2 = (ps[1] * ps[1] / 3.) * voli, m3 = (ps[2] * ps[2] / 3.) * voli;
   k_grid_acc<D, R, EX, 3><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, m1, m2, m3, Q);
+  /* the inline solve of a stage that outgrew the queue (returns at once otherwise) */
+  k_grid_acc<D, R, EX, 0><<<grid_for(K.ncell, 128), 128, 0, st>>>(K, P, K.mgfm_variant, voli, m1, m2, m3, Q);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1199,18 +1227,69 @@ void Launch<D, R, EX>::update_grid(const CaseK& K, const DevPtrs<R>& P, int md, 
 /* ------------------------------------------------------------------ */
 /* conservation totals (Triple_point_2phase/mpm_ini.cpp:599-654)       */
 /* ------------------------------------------------------------------ */
+/* Sums in double-double (an error-free TwoSum of each addend, the errors summed
+ * beside the running sum: Neumaier's compensated summation), rounded once: the
+ * result agrees with the exactly rounded sum but for sums within about
+ * n^2 eps^2 of a rounding boundary, whatever the order of the addends, so the
+ * parallel reduction here and the oracle's serial loop give the same double.
+ * (Internal linkage: this file is compiled twice, for the exact and the other
+ * paths.) */
+namespace {
+struct DD {
+  double hi, lo;
+};
+__device__ __forceinline__ void dd_add(DD& a, double b) {
+  const double s = a.hi + b;
+  const double bb = s - a.hi;
+  a.lo += (a.hi - (s - bb)) + (b - bb);
+  a.hi = s;
+}
+__device__ __forceinline__ void dd_merge(DD& a, const DD& b) {
+  dd_add(a, b.hi);
+  a.lo += b.lo;
+}
+constexpr int TOT_BLOCKS = 304, TOT_THREADS = 256;
+constexpr size_t PROBE_DOUBLES = 6 * (size_t)TOT_BLOCKS; /* the bubble probe's block partials */
+/* the blocks' partial sums in block order, rounded once */
+__global__ void k_totals_final(const DD* part, double* out) {
+  if (threadIdx.x < 6) {
+    DD t = part[threadIdx.x];
+    for (int b = 1; b < TOT_BLOCKS; b++) dd_merge(t, part[b * 6 + threadIdx.x]);
+    out[threadIdx.x] = t.hi + t.lo;
+  }
+}
+__global__ void k_probe_final(const double* part, double* out) {
+  if (threadIdx.x == 0) {
+    double r[6] = {part[0], part[1], part[2], 0, 0, part[5]};
+    DD m{part[3], part[4]};
+    for (int b = 1; b < TOT_BLOCKS; b++) {
+      r[0] = fmax(r[0], part[b * 6 + 0]);
+      r[1] = fmin(r[1], part[b * 6 + 1]);
+      r[2] = fmin(r[2], part[b * 6 + 2]);
+      dd_merge(m, DD{part[b * 6 + 3], part[b * 6 + 4]});
+      r[5] += part[b * 6 + 5];
+    }
+    out[0] = r[0];
+    out[1] = r[1];
+    out[2] = r[2];
+    out[3] = m.hi + m.lo;
+    out[4] = r[5];
+  }
+}
+}  // namespace
+
 template <int D, typename R, bool EX>
-__global__ void k_totals(CaseK K, DevPtrs<R> P, double* out) {
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+__global__ void __launch_bounds__(TOT_THREADS) k_totals(CaseK K, DevPtrs<R> P, DD* part) {
+  DD acc[6];
+  for (int k = 0; k < 6; k++) acc[k] = DD{0.0, 0.0};
   const int64_t n = (int64_t)P.cnt->n_slots;
   GRID_STRIDE(p, n) {
     int ph = P.phase[p];
     if (ph == 0) continue;
-    double m = (double)P.rho[p] * (double)P.vol[p];
-    acc[ph - 1] += m;
+    dd_add(acc[ph - 1], (double)P.rho[p] * (double)P.vol[p]);
     double e = (double)P.E[p];
     if (K.eshift[ph - 1] != 0.0) e += K.eshift[ph - 1];
-    acc[2] += e * (double)P.vol[p];
+    dd_add(acc[2], e * (double)P.vol[p]);
   }
   const int64_t nc = K.ncell;
   double voli = K.ps[0] * K.ps[1] * (D == 3 ? K.ps[2] : 1.0);
@@ -1219,23 +1298,118 @@ __global__ void k_totals(CaseK K, DevPtrs<R> P, double* out) {
     for (int s = 0; s < F; s++) {
       if (P.cph[s * nc + ci] != 1) continue;
       double a = (double)P.calph[s * nc + ci];
-      acc[3 + s] += voli * a * (double)P.crho[s * nc + ci];
+      dd_add(acc[3 + s], voli * a * (double)P.crho[s * nc + ci]);
       double e = (double)P.cE[s * nc + ci];
       if (K.eshift[s] != 0.0) e += K.eshift[s];
-      acc[5] += voli * a * e;
+      dd_add(acc[5], voli * a * e);
     }
   }
+  __shared__ DD s_w[TOT_THREADS / 32][6];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int k = 0; k < 6; k++) {
-    double v = acc[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&out[k], v);
+    for (int o = 16; o > 0; o >>= 1) {
+      DD b{__shfl_down_sync(0xffffffffu, acc[k].hi, o), __shfl_down_sync(0xffffffffu, acc[k].lo, o)};
+      if (lane + o < 32) dd_merge(acc[k], b);
+    }
+    if (lane == 0) s_w[w][k] = acc[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    DD t = s_w[0][threadIdx.x];
+    for (int v = 1; v < TOT_THREADS / 32; v++) dd_merge(t, s_w[v][threadIdx.x]);
+    part[blockIdx.x * 6 + threadIdx.x] = t;
   }
 }
 
 template <int D, typename R, bool EX>
 void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out6, cudaStream_t st) {
-  cudaMemsetAsync(d_out6, 0, 6 * sizeof(double), st);
-  k_totals<D, R, EX><<<grid_for(K.cap > K.ncell ? K.cap : K.ncell, BLK), BLK, 0, st>>>(K, P, d_out6);
+  /* d_out6 holds 6 results followed by the blocks' partials (totals_scratch) */
+  DD* part = reinterpret_cast<DD*>(d_out6 + 6);
+  k_totals<D, R, EX><<<TOT_BLOCKS, TOT_THREADS, 0, st>>>(K, P, part);
+  k_totals_final<<<1, 32, 0, st>>>(part, d_out6);
+}
+template <int D, typename R, bool EX>
+size_t Launch<D, R, EX>::totals_scratch() {
+  return 6 + 2 * 6 * (size_t)TOT_BLOCKS + PROBE_DOUBLES;
+}
+
+/* ------------------------------------------------------------------ */
+/* bubble probe (Output_point, mpm_ini.cpp:774-824)                   */
+/* ------------------------------------------------------------------ */
+/* Over the phase-2 particles: the largest and smallest x of those near the
+ * axis (y and z below 2.5 p_sz: the bubble's downstream end and the jet) and
+ * the smallest x of those away from it (y or z above 4 p_sz: the upstream
+ * end), the phase-2 mass sum rho vol, and the number of fluid particles.
+ * Per-block partials, combined in block order (deterministic). */
+template <int D, typename R, bool EX>
+__global__ void __launch_bounds__(TOT_THREADS) k_probe(CaseK K, DevPtrs<R> P, double* part) {
+  double dw = K.bl[0], jet = K.br[0], ups = K.br[0];
+  DD mass{0.0, 0.0};
+  unsigned long long cnt = 0;
+  const R* X = P.X[P.xb];
+  const double a = 2.5 * K.p_sz, b = 4 * K.p_sz;
+  const int64_t n = (int64_t)P.cnt->n_slots;
+  GRID_STRIDE(p, n) {
+    const int ph = P.phase[p];
+    if (ph == 0) continue;
+    cnt++;
+    if (ph != 2) continue;
+    const double x = (double)X[p], y = (double)X[K.cap + p], z = D == 3 ? (double)X[2 * K.cap + p] : 0.0;
+    if (y < a && z < a) {
+      dw = fmax(dw, x);
+      jet = fmin(jet, x);
+    } else if (y > b || z > b) {
+      ups = fmin(ups, x);
+    }
+    dd_add(mass, (double)P.rho[p] * (double)P.vol[p]);
+  }
+  __shared__ double s_v[TOT_THREADS / 32][6];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double c = (double)cnt;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double dw2 = __shfl_down_sync(0xffffffffu, dw, o), jet2 = __shfl_down_sync(0xffffffffu, jet, o);
+    const double ups2 = __shfl_down_sync(0xffffffffu, ups, o);
+    DD m2{__shfl_down_sync(0xffffffffu, mass.hi, o), __shfl_down_sync(0xffffffffu, mass.lo, o)};
+    const double c2 = __shfl_down_sync(0xffffffffu, c, o);
+    if (lane + o < 32) {
+      dw = fmax(dw, dw2);
+      jet = fmin(jet, jet2);
+      ups = fmin(ups, ups2);
+      dd_merge(mass, m2);
+      c += c2;
+    }
+  }
+  if (lane == 0) {
+    s_v[w][0] = dw;
+    s_v[w][1] = jet;
+    s_v[w][2] = ups;
+    s_v[w][3] = mass.hi;
+    s_v[w][4] = mass.lo;
+    s_v[w][5] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r[6] = {s_v[0][0], s_v[0][1], s_v[0][2], 0, 0, s_v[0][5]};
+    DD m{s_v[0][3], s_v[0][4]};
+    for (int v = 1; v < TOT_THREADS / 32; v++) {
+      r[0] = fmax(r[0], s_v[v][0]);
+      r[1] = fmin(r[1], s_v[v][1]);
+      r[2] = fmin(r[2], s_v[v][2]);
+      dd_merge(m, DD{s_v[v][3], s_v[v][4]});
+      r[5] += s_v[v][5];
+    }
+    r[3] = m.hi;
+    r[4] = m.lo;
+    for (int k = 0; k < 6; k++) part[blockIdx.x * 6 + k] = r[k];
+  }
+}
+template <int D, typename R, bool EX>
+void Launch<D, R, EX>::probe(const CaseK& K, const DevPtrs<R>& P, double* d_scratch, double* d_out5,
+                             cudaStream_t st) {
+  /* d_scratch: the totals scratch; the probe's partials use its last PROBE_DOUBLES */
+  double* part = d_scratch + totals_scratch() - PROBE_DOUBLES;
+  k_probe<D, R, EX><<<TOT_BLOCKS, TOT_THREADS, 0, st>>>(K, P, part);
+  k_probe_final<<<1, 32, 0, st>>>(part, d_out5);
 }
 
 #define PGDG_INST(D, R, EX)                                                                     \
@@ -1246,10 +1420,12 @@ void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out
   template void Launch<D, R, EX>::p2g_new(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \
   template void Launch<D, R, EX>::limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);          \
   template void Launch<D, R, EX>::grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);         \
-  template int64_t Launch<D, R, EX>::iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t); \
+  template void Launch<D, R, EX>::iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t); \
   template void Launch<D, R, EX>::grid_acc_queued(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t); \
   template void Launch<D, R, EX>::update_grid(const CaseK&, const DevPtrs<R>&, int, cudaStream_t); \
-  template void Launch<D, R, EX>::totals(const CaseK&, const DevPtrs<R>&, double*, cudaStream_t);
+  template void Launch<D, R, EX>::totals(const CaseK&, const DevPtrs<R>&, double*, cudaStream_t);  \
+  template size_t Launch<D, R, EX>::totals_scratch();                                             \
+  template void Launch<D, R, EX>::probe(const CaseK&, const DevPtrs<R>&, double*, double*, cudaStream_t);
 #ifdef PGDG_EXACT_TU
 PGDG_INST(2, double, true)
 PGDG_INST(3, double, true)

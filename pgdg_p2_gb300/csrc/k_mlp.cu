@@ -179,7 +179,8 @@ __device__ __forceinline__ void mlp_eval(const float* w, const float* xn, float*
 template <bool BF16>
 __global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ params, const float* __restrict__ X,
                                                      float* __restrict__ Y, float* A1, float* A2, float* A3,
-                                                     int64_t n) {
+                                                     int64_t n, const unsigned long long* __restrict__ dn) {
+  if (dn && (int64_t)*dn < n) n = (int64_t)*dn; /* live count of a batch sized for capacity */
   __shared__ __align__(16) float w[NPARAM + NNORM];
   load_params<BF16>(params, w);
   const float* mx = w + NPARAM;
@@ -282,9 +283,12 @@ __device__ __forceinline__ double mgfm_f(double ul, double ur, double pl, double
   return ul - ur - (p - pl) / Wl - (p - pr) / Wr;
 }
 
-/* the seed from the baseline, the strength scale and the network output */
+/* the seed from the baseline, the strength scale and the network output; an
+ * output far outside the training range that overflows the exponential gives
+ * -1, the plain seed */
 __device__ __forceinline__ double seed_value(double pb, float sc, float y0, float my0, float sy0) {
   const double ps = pb * (double)expf(sc * (y0 * sy0 + my0));
+  if (!isfinite(ps)) return -1.0;
   return ps > 1e-8 ? ps : 1e-8;
 }
 
@@ -334,7 +338,8 @@ __global__ void __launch_bounds__(128) k_seed(const float* __restrict__ params, 
 __global__ void k_seed_features(const double* __restrict__ in6, const int8_t* __restrict__ mat2,
                                 const double* __restrict__ gam, const double* __restrict__ pinf, int variant,
                                 float* __restrict__ X, double* __restrict__ pb_out, float* __restrict__ sc_out,
-                                int64_t n) {
+                                int64_t n, const unsigned long long* __restrict__ dn) {
+  if (dn && (int64_t)*dn < n) n = (int64_t)*dn;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double* q = in6 + 6 * i;
     const int s = mat2[2 * i], s1 = mat2[2 * i + 1];
@@ -369,7 +374,9 @@ __global__ void k_seed_features(const double* __restrict__ in6, const int8_t* __
  * path computed it, else f(1e-8) >= 0 evaluated here). */
 __global__ void k_root_flag(const double* __restrict__ in6, const int8_t* __restrict__ mat2,
                             const double* __restrict__ gam, const double* __restrict__ pinf, int variant,
-                            const double* __restrict__ pb, unsigned long long* __restrict__ flag, int64_t n) {
+                            const double* __restrict__ pb, unsigned long long* __restrict__ flag, int64_t n,
+                            const unsigned long long* __restrict__ dn) {
+  if (dn && (int64_t)*dn < n) n = (int64_t)*dn;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     bool root;
     if (pb) {
@@ -395,7 +402,8 @@ __global__ void k_root_flag(const double* __restrict__ in6, const int8_t* __rest
 /* order: problems with a root first, then the others, each in input order;
  * pos is the exclusive prefix of the flags, nroot_p their total */
 __global__ void k_root_perm(const unsigned long long* __restrict__ pos, const unsigned long long* __restrict__ nroot_p,
-                            int32_t* __restrict__ perm, int64_t n) {
+                            int32_t* __restrict__ perm, int64_t n, const unsigned long long* __restrict__ dn) {
+  if (dn && (int64_t)*dn < n) n = (int64_t)*dn;
   const int64_t nroot = (int64_t)*nroot_p;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = (int64_t)pos[i];
@@ -412,7 +420,9 @@ __global__ void k_mgfm_seeded(const double* __restrict__ in6, const int8_t* __re
                               const double* __restrict__ seed, double* __restrict__ out3, int32_t* __restrict__ iters,
                               int64_t n, unsigned long long* stats, const float* __restrict__ Y,
                               const float* __restrict__ sc, const float* __restrict__ params,
-                              const int32_t* __restrict__ perm, const int* __restrict__ yerr) {
+                              const int32_t* __restrict__ perm, const int* __restrict__ yerr,
+                              const unsigned long long* __restrict__ dn) {
+  if (dn && (int64_t)*dn < n) n = (int64_t)*dn;
   unsigned long long nit = 0, nmax = 0, ncall = 0;
   /* a tensor-core forward pass that gave up leaves Y unset: every problem then
    * starts from the plain seed (the reference's), so results stay valid */
@@ -432,7 +442,10 @@ __global__ void k_mgfm_seeded(const double* __restrict__ in6, const int8_t* __re
     bool done = false;
     if (sd > 0) {
       it = mgfm(q[0], q[1], q[2], q[3], q[4], q[5], gam[s], pinf[s], gam[s1], pinf[s1], variant, sd, o);
-      done = it < 50;
+      /* a seeded solve is kept only when it converged to finite values (a
+       * non-finite iterate fails the tolerance test and would leave the loop
+       * early); otherwise the problem is solved again from the plain seed */
+      done = it < 50 && isfinite(o[0]) && isfinite(o[1]) && isfinite(o[2]);
     }
     if (!done) it += mgfm(q[0], q[1], q[2], q[3], q[4], q[5], gam[s], pinf[s], gam[s1], pinf[s1], variant, -1.0, o);
     out3[3 * i + 0] = o[0];
@@ -472,16 +485,18 @@ struct pgdg_mlp {
   PartScratch part;         /* root partition of batched solves */
   double* seeds = nullptr; /* per-problem seeds (or baselines) of batched solves */
   float* sc = nullptr;     /* per-problem strength scale of the split seed path */
+  float *Xb = nullptr, *Yb = nullptr; /* features and network outputs of batched solves */
   int64_t seeds_cap = 0;
   int reserve_seeds(int64_t n) {
     if (n <= seeds_cap) return PGDG_OK;
-    if (seeds) cudaFree(seeds);
-    if (sc) cudaFree(sc);
-    seeds = nullptr;
-    sc = nullptr;
+    void** bufs[] = {(void**)&seeds, (void**)&sc, (void**)&Xb, (void**)&Yb};
+    const size_t w[] = {sizeof(double), sizeof(float), sizeof(float) * NI, sizeof(float) * NO};
     seeds_cap = 0;
-    if (cudaMalloc((void**)&seeds, sizeof(double) * n) != cudaSuccess) return PGDG_ENOMEM;
-    if (cudaMalloc((void**)&sc, sizeof(float) * n) != cudaSuccess) return PGDG_ENOMEM;
+    for (int k = 0; k < 4; k++) {
+      if (*bufs[k]) cudaFree(*bufs[k]);
+      *bufs[k] = nullptr;
+      if (cudaMalloc(bufs[k], w[k] * (size_t)n) != cudaSuccess) return PGDG_ENOMEM;
+    }
     seeds_cap = n;
     return PGDG_OK;
   }
@@ -503,6 +518,8 @@ struct pgdg_mlp {
     if (d_loss) cudaFree(d_loss);
     if (seeds) cudaFree(seeds);
     if (sc) cudaFree(sc);
+    if (Xb) cudaFree(Xb);
+    if (Yb) cudaFree(Yb);
     if (d_tcerr) cudaFree(d_tcerr);
     part.release();
   }
@@ -514,15 +531,16 @@ inline int g_for(int64_t n, int b) {
   if (g > 152 * 16) g = 152 * 16;
   return g < 1 ? 1 : (int)g;
 }
-void forward(pgdg_mlp* m, const float* X, float* Y, float* A1, float* A2, float* A3, int64_t n, cudaStream_t st) {
+void forward(pgdg_mlp* m, const float* X, float* Y, float* A1, float* A2, float* A3, int64_t n, cudaStream_t st,
+             const unsigned long long* dn = nullptr) {
   if (m->tc && !A1) {
     /* the flag reports this forward pass only */
     cudaMemsetAsync(m->d_tcerr, 0, sizeof(int), st);
-    mlp_tc_forward(m->d_params, X, Y, n, m->d_tcerr, st);
+    mlp_tc_forward(m->d_params, X, Y, n, m->d_tcerr, st, dn);
     return;
   }
-  if (m->bf16) k_mlp_forward<true><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n);
-  else k_mlp_forward<false><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n);
+  if (m->bf16) k_mlp_forward<true><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n, dn);
+  else k_mlp_forward<false><<<g_for(n, 128), 128, 0, st>>>(m->d_params, X, Y, A1, A2, A3, n, dn);
 }
 void seed_launch(pgdg_mlp* m, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
                  int variant, double* seed, int64_t n, cudaStream_t st) {
@@ -653,13 +671,13 @@ int pgdg_mgfm_batched(const pgdg_mlp* net, const double* in6, const int8_t* mat2
   /* partition scratch: the network's, or (plain seed) a per-device cache used
    * under a lock; calls run on the default stream */
   if (net) return mgfm_seeded_run((void*)net, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr,
-                                  const_cast<pgdg_mlp*>(net)->part, 0);
+                                  const_cast<pgdg_mlp*>(net)->part, 0, nullptr);
   static PartScratch cache[64];
   static std::mutex mu;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PGDG_ECUDA;
   std::lock_guard<std::mutex> lk(mu);
-  return mgfm_seeded_run(nullptr, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr, cache[dev], 0);
+  return mgfm_seeded_run(nullptr, in6, mat2, gam, pinf, variant, out3, iters, n, nullptr, cache[dev], 0, nullptr);
 }
 
 /* Seeds of pgdg_mgfm_batched_noalloc: a file-scope device array, so the call
@@ -694,7 +712,7 @@ int pgdg_mgfm_batched_noalloc(const pgdg_mlp* net, const double* in6, const int8
     sd = seeds;
   }
   k_mgfm_seeded<<<g_for(n, 256), 256>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, nullptr, nullptr, nullptr,
-                                        nullptr, nullptr, nullptr);
+                                        nullptr, nullptr, nullptr, nullptr);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 
@@ -728,9 +746,15 @@ void PartScratch::release() {
   cap = 0;
 }
 
+int mgfm_seeded_reserve(void* netv, PartScratch& ps, int64_t n) {
+  int rc = ps.reserve(n);
+  if (rc == PGDG_OK && netv) rc = static_cast<pgdg_mlp*>(netv)->reserve_seeds(n);
+  return rc;
+}
+
 int mgfm_seeded_run(void* netv, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
                     int variant, double* out3, int32_t* iters, int64_t n, unsigned long long* stats,
-                    PartScratch& ps, cudaStream_t st) {
+                    PartScratch& ps, cudaStream_t st, const unsigned long long* dn) {
   if (n <= 0) return PGDG_OK;
   if (n > INT32_MAX) return PGDG_EINVAL;
   pgdg_mlp* m = static_cast<pgdg_mlp*>(netv);
@@ -742,23 +766,23 @@ int mgfm_seeded_run(void* netv, const double* in6, const int8_t* mat2, const dou
      * seed formed per problem (same arithmetic as the fused k_seed) */
     rc = m->reserve_seeds(n);
     if (rc) return rc;
-    rc = m->reserve(n);
-    if (rc) return rc;
-    k_seed_features<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, m->X, m->seeds, m->sc, n);
-    forward(m, m->X, m->Y, nullptr, nullptr, nullptr, n, st);
+    k_seed_features<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, m->Xb, m->seeds, m->sc, n, dn);
+    forward(m, m->Xb, m->Yb, nullptr, nullptr, nullptr, n, st, dn);
     sd = m->seeds;
   }
   /* problems with a root first: warps of converging problems are not held up
    * by the long floor descent of problems without one (results per problem
    * are unchanged) */
-  const unsigned long long nn = (unsigned long long)n;
-  cudaMemcpyAsync(ps.dn, &nn, sizeof(nn), cudaMemcpyHostToDevice, st);
-  k_root_flag<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, ps.pos, n);
-  scan_u64(ps.pos, ps.blk, ps.dn, n, st);
-  k_root_perm<<<g_for(n, 256), 256, 0, st>>>(ps.pos, ps.blk + (n + 2047) / 2048, ps.perm, n);
+  if (!dn) {
+    const unsigned long long nn = (unsigned long long)n;
+    cudaMemcpyAsync(ps.dn, &nn, sizeof(nn), cudaMemcpyHostToDevice, st);
+  }
+  k_root_flag<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, ps.pos, n, dn);
+  scan_u64(ps.pos, ps.blk, dn ? dn : ps.dn, n, st);
+  k_root_perm<<<g_for(n, 256), 256, 0, st>>>(ps.pos, ps.blk + (n + 2047) / 2048, ps.perm, n, dn);
   k_mgfm_seeded<<<g_for(n, 256), 256, 0, st>>>(in6, mat2, gam, pinf, variant, sd, out3, iters, n, stats,
-                                               m ? m->Y : nullptr, m ? m->sc : nullptr, m ? m->d_params : nullptr,
-                                               ps.perm, m && m->tc ? m->d_tcerr : nullptr);
+                                               m ? m->Yb : nullptr, m ? m->sc : nullptr, m ? m->d_params : nullptr,
+                                               ps.perm, m && m->tc ? m->d_tcerr : nullptr, dn);
   return cudaGetLastError() == cudaSuccess ? PGDG_OK : PGDG_ECUDA;
 }
 }  // namespace pgdg

@@ -156,7 +156,9 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t trow, const float* bias
 }  // namespace
 
 __global__ void __launch_bounds__(128, 4) k_mlp_tc(const float* __restrict__ params, const float* __restrict__ X,
-                                                   float* __restrict__ Y, int64_t n, int* __restrict__ err) {
+                                                   float* __restrict__ Y, int64_t n, int* __restrict__ err,
+                                                   const unsigned long long* __restrict__ dn) {
+  if (dn && (int64_t)*dn < n) n = (int64_t)*dn; /* live count of a batch sized for capacity */
   extern __shared__ __align__(1024) unsigned char sm[];
   const int t = threadIdx.x, warp = t >> 5;
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
@@ -279,11 +281,12 @@ __global__ void __launch_bounds__(128, 4) k_mlp_tc(const float* __restrict__ par
 }
 
 /* launch over n problems; err: device flag set when a wait gave up */
-int mlp_tc_forward(const float* params, const float* X, float* Y, int64_t n, int* err, cudaStream_t st) {
+int mlp_tc_forward(const float* params, const float* X, float* Y, int64_t n, int* err, cudaStream_t st,
+                   const unsigned long long* dn) {
   if (n <= 0) return 0;
   const int64_t ntile = (n + TILE - 1) / TILE;
   const int grid = (int)(ntile < 152 * 4 ? ntile : 152 * 4);
-  k_mlp_tc<<<grid, 128, S_TOTAL, st>>>(params, X, Y, n, err);
+  k_mlp_tc<<<grid, 128, S_TOTAL, st>>>(params, X, Y, n, err, dn);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

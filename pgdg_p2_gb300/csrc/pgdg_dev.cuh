@@ -143,6 +143,9 @@ struct IfaceQ {
   unsigned long long* off;
   unsigned long long* blk;
   const unsigned long long* d_ncell;
+  /* [0] the stage's interface problems, [1] those the batch solves: [0], or 0
+   * when [0] exceeds cap (the residual then solves the stage inline) */
+  unsigned long long* tot;
   int64_t cap;
 };
 
@@ -215,10 +218,14 @@ struct Launch {
   static void limiter(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   static void grid_acc(const CaseK&, const DevPtrs<R>&, cudaStream_t);
   /* queued variant: returns the number of interface problems (negative: over capacity) */
-  static int64_t iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t);
+  static void iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t);
   static void grid_acc_queued(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t);
   static void update_grid(const CaseK&, const DevPtrs<R>&, int md, cudaStream_t);
   static void totals(const CaseK&, const DevPtrs<R>&, double* d_out6, cudaStream_t);
+  static size_t totals_scratch(); /* doubles d_out6 must hold */
+  /* bubble probe (downstream end, jet, upstream end, phase-2 mass, fluid
+   * count) into d_out5, with the totals scratch for its partials */
+  static void probe(const CaseK&, const DevPtrs<R>&, double* d_scratch, double* d_out5, cudaStream_t);
   /* k_g2p.cu */
   /* xs/hs: stage-start coordinate/h buffers, x0: step-start coordinates (md 1),
    * xn/hn: buffers receiving the new coordinates/h */
@@ -268,9 +275,11 @@ void fill_dev(R* d, int64_t n, R v, cudaStream_t st);
 void alive_index(const int8_t* phase, unsigned long long* scan, unsigned long long* blk,
                  const unsigned long long* d_n, int64_t cap, int64_t* idx, cudaStream_t st);
 
-/* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls, iterations, cap hits) */
-/* forward pass of the seed surrogate on the tensor cores (k_mlp_tc.cu) */
-int mlp_tc_forward(const float* params, const float* X, float* Y, int64_t n, int* err, cudaStream_t st);
+/* forward pass of the seed surrogate on the tensor cores (k_mlp_tc.cu); with
+ * dn, a batch launched for n entries whose live count *dn (<= n) is known on
+ * the device only */
+int mlp_tc_forward(const float* params, const float* X, float* Y, int64_t n, int* err, cudaStream_t st,
+                   const unsigned long long* dn = nullptr);
 
 /* scratch of the root partition of a batch (prefix, block sums, order, count) */
 struct PartScratch {
@@ -280,9 +289,22 @@ struct PartScratch {
   int reserve(int64_t n);
   void release();
 };
+/* seeded batched MGFM over device buffers (k_mlp.cu); stats += (calls,
+ * iterations, cap hits).  Launches are sized for n; with dn the batch's live
+ * count is *dn (clamped to n), read on the device, so the call reads nothing
+ * back on the host and can be captured in a graph once its scratch holds n */
 int mgfm_seeded_run(void* net, const double* in6, const int8_t* mat2, const double* gam, const double* pinf,
                     int variant, double* out3, int32_t* iters, int64_t n, unsigned long long* stats,
-                    PartScratch& ps, cudaStream_t st);
+                    PartScratch& ps, cudaStream_t st, const unsigned long long* dn);
+/* allocate the scratch a batch of n needs (partition and, with a network, seeds
+ * and features) ahead of a capture, so the captured call allocates nothing */
+int mgfm_seeded_reserve(void* net, PartScratch& ps, int64_t n);
+
+/* the synthetic workload id built in place on the device (k_case.cu): n
+ * lattice particles and every cell, as the host builder makes them */
+template <int D, typename R>
+int case_build(const CaseK& K, const DevPtrs<R>& P, const pgdg_case& cs, int id, uint64_t seed, int64_t n,
+               cudaStream_t st);
 
 /* minimum resident 128-thread blocks per SM asked of the FP32 instantiations of
  * the per-cell and per-particle kernels (a register cap that trades a few

@@ -58,6 +58,8 @@ def lib():
         L.pgdg_run_step.argtypes = [vp, C.c_int64]
         L.pgdg_advance.argtypes = [vp, C.c_int]
         L.pgdg_totals.argtypes = [vp, P(C.c_double)]
+        L.pgdg_output_point.argtypes = [vp, P(C.c_double)]
+        L.pgdg_case_build.argtypes = [vp, C.c_int, C.c_uint64]
         L.pgdg_profile.argtypes = [vp, C.c_int]
         L.pgdg_profile_read.argtypes = [vp, C.c_char_p, C.c_int, P(C.c_double), P(C.c_int64), C.c_int, P(C.c_int)]
         L.pgdg_launch_count.argtypes = [vp, P(C.c_int64)]
@@ -144,6 +146,10 @@ class MPM:
         self._ck(lib().pgdg_synchronize(self.h), "pgdg_synchronize")
 
     # ---- state exchange ----
+    def case_build(self, config_id, seed=0):
+        """Build workload config_id (this context's case) in place on the device."""
+        self._ck(lib().pgdg_case_build(self.h, int(config_id), int(seed)), "case_build")
+
     def upload_particles(self, p: Particles):
         v = p.view()
         v.n = p.n
@@ -248,6 +254,12 @@ class MPM:
         s = pgdg_stats()
         self._ck(lib().pgdg_get_stats(self.h, C.byref(s)), "stats")
         return s.to_dict()
+
+    def output_point(self):
+        """Output_point's bubble probe: (downstream end, jet, upstream end, phase-2 mass, fluid count)."""
+        out = np.zeros(5)
+        self._ck(lib().pgdg_output_point(self.h, out.ctypes.data_as(C.POINTER(C.c_double))), "output_point")
+        return out
 
     def totals(self):
         out = np.zeros(6)

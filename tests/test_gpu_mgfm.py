@@ -44,3 +44,24 @@ def test_mgfm_bitwise_random(gpu_mod, oracle_mod, variant):
     oo, io = oracle_mod.mgfm_batched(in6, mat, gam, pinf, variant)
     assert np.array_equal(ig, io)
     assert og.tobytes() == oo.tobytes()
+
+
+@pytest.mark.parametrize("tc", [False, True])
+def test_overflowing_seed_falls_back_to_plain(gpu_mod, tc):
+    """A network whose output overflows the seed's exponential (here an output
+    mean of 1e30) must leave every problem to the plain solve: the same
+    results as no network, bit for bit."""
+    from pgdg_p2_gb300 import surrogate as S
+    from tests.golden.make_golden import mgfm_inputs
+    in6, mat = mgfm_inputs(np.random.default_rng(5), 1 << 14)
+    gam = np.array([1.4, 1.648, 7.15, 2.0])
+    pinf = np.array([0.0, 0.0, 3.309e8, 0.0])
+    p = S.baseline_params()
+    p[S.NPARAM + 2 * S.NI] = 1e30
+    net = S.Surrogate(p, tc=tc)
+    out, it = S.mgfm_gpu(in6, mat, gam, pinf, net)
+    net.close()
+    ref, it_ref = S.mgfm_gpu(in6, mat, gam, pinf, None)
+    assert np.all(np.isfinite(out))
+    assert out.tobytes() == ref.tobytes()
+    assert np.all(it >= it_ref)

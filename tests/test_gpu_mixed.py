@@ -49,7 +49,7 @@ def test_mixed_shift_vs_oracle(gpu_mod, oracle_mod, cid, grid):
 # warp-cooperative one (1, boundary particles in a second pass) in the same
 # order, so they differ at most by rounding from the order of the boundary sums
 TOL_VARIANTS = 1e-6
-PST_VARIANTS = 6
+PST_VARIANTS = 8
 
 
 def _shift_after_one_step(M, cs, p, c, prec, variant):

@@ -107,6 +107,22 @@ int pgdg_totals(pgdg_ctx* ctx, double* out6);
  * number of fluid particles (the rows of pointa.txt and mass.txt); the ends
  * start at the box's left and right x */
 int pgdg_output_point(pgdg_ctx* ctx, double* out5);
+/* MPM::Output_plt_file (mpm_ini.cpp:832-980): the live particles as a Tecplot
+ * binary (#!TDV112, one ordered zone of twelve variables x y z phase vx vy vol
+ * rho P |tv| |v| n_neighbor, doubles with phase and n_neighbor int32, stored
+ * variable after variable in canonical order) and the cells as the ASCII table
+ * (centre, v1 v2 |v|, rho0 rho1, coef[0](1,1) coef[0](1,2), Lim_u[0](0)
+ * Lim_u[1](0), alph0 alph1, P; one line per cell, i outer); either path may be
+ * NULL.  The solution time is the context's simulated time.  n_neighbor is the
+ * flag-2 list size (fluid and boundary particles within 2h, itself included)
+ * over the last stage's search coordinates, or the current ones when the
+ * particle set changed since.  The state is packed on the device into a
+ * snapshot; with async = 0 the call returns once both files are written, with
+ * async = 1 as soon as the snapshot is packed, a host thread copying it out and
+ * writing while later calls go on (pgdg_output_wait joins it and returns its
+ * status; the next pgdg_output_plt and pgdg_destroy wait for it too). */
+int pgdg_output_plt(pgdg_ctx* ctx, const char* particle_path, const char* cell_path, int async);
+int pgdg_output_wait(pgdg_ctx* ctx);
 
 /* ---- MGFM seed surrogate (new; the reference starts Newton from max(p_l,p_r),
  *      mpm.cpp:893) ----

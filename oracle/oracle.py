@@ -52,6 +52,7 @@ def lib():
         L.po_advance.argtypes = [vp, C.c_int]
         L.po_totals.argtypes = [vp, P(C.c_double)]
         L.po_output_point.argtypes = [vp, P(C.c_double)]
+        L.po_output_plt.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.po_set_threads.argtypes = [C.c_int]
         L.po_mgfm_batched.argtypes = [P(C.c_double), P(C.c_int8), P(C.c_double), P(C.c_double), C.c_int,
                                       P(C.c_double), P(C.c_double), P(C.c_int32), C.c_int64]
@@ -220,6 +221,13 @@ class Oracle:
         out = np.zeros(5)
         lib().po_output_point(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
+
+    def output_plt(self, particle_path=None, cell_path=None):
+        """Output_plt_file: the particle Tecplot binary and the cell table."""
+        enc = (lambda p: str(p).encode() if p is not None else None)
+        rc = lib().po_output_plt(self.h, enc(particle_path), enc(cell_path))
+        if rc != 0:
+            raise RuntimeError(f"po_output_plt failed ({rc})")
 
     def totals(self):
         out = np.zeros(6)

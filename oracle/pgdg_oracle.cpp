@@ -26,6 +26,8 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <fstream>
+#include <string>
 #include <unordered_set>
 #include <vector>
 #ifdef _OPENMP
@@ -59,6 +61,7 @@ struct po_ctx {
   virtual void run_step(int64_t n) = 0;
   virtual void totals(double* out) = 0;
   virtual void output_point(double* out) = 0;
+  virtual int output_plt(const char* ppath, const char* cpath) = 0;
   double dt = 0, max_v = 1e-7;
   int64_t iterate = 0;
   pgdg_stats st{};
@@ -1496,6 +1499,100 @@ struct OracleT : po_ctx {
     out[0] = pm[0].value(); out[1] = pm[1].value(); out[2] = pe.value();
     out[3] = cm[0].value(); out[4] = cm[1].value(); out[5] = ce.value();
   }
+  /* MPM::Output_plt_file (mpm_ini.cpp:832-980): the particles as a Tecplot
+   * binary (#!TDV112, one ordered zone, twelve variables stored one after the
+   * other, doubles and int32) and the cells as an ASCII table written through
+   * an ostream in its default format.  Test infrastructure: the reference for
+   * the library's writer. */
+  template <class T>
+  static void put(std::ofstream& o, T v) { o.write(reinterpret_cast<const char*>(&v), sizeof(v)); }
+  static void put_name(std::ofstream& o, const char* s) {
+    /* each character as an int32, then a 0 */
+    for (const char* c = s; *c; c++) put<int32_t>(o, (int32_t)(unsigned char)*c);
+    put<int32_t>(o, 0);
+  }
+  int output_plt(const char* ppath, const char* cpath) override {
+    if (ppath) {
+      std::ofstream o(ppath, std::ios::binary);
+      if (!o) return PGDG_EINVAL;
+      o.write("#!TDV112", 8);
+      put<int32_t>(o, 1);
+      put<int32_t>(o, 0);
+      put<int32_t>(o, 0);
+      static const char* names[12] = {"x", "y", "z", "phase", "vx", "vy", "vol", "rho", "P", "tv", "v", "n_neighbor"};
+      static const int32_t types[12] = {2, 2, 2, 3, 2, 2, 2, 2, 2, 2, 2, 3};
+      put<int32_t>(o, 12);
+      for (auto n : names) put_name(o, n);
+      put<float>(o, 299.0f);
+      put_name(o, "grid");
+      put<int32_t>(o, -1);
+      put<int32_t>(o, 0);
+      put<double>(o, st.time);
+      put<int32_t>(o, -1);
+      put<int32_t>(o, 0);
+      put<int32_t>(o, 0);
+      put<int32_t>(o, 0);
+      put<int32_t>(o, 0);
+      put<int32_t>(o, (int32_t)fluid.size());
+      put<int32_t>(o, 1);
+      put<int32_t>(o, 1);
+      put<int32_t>(o, 0);
+      put<float>(o, 357.0f);
+      put<float>(o, 299.0f);
+      for (auto t : types) put<int32_t>(o, t);
+      put<int32_t>(o, 0);
+      put<int32_t>(o, 0);
+      put<int32_t>(o, -1);
+      for (int j = 0; j < 12; j++) {
+        put<double>(o, -1.0);
+        put<double>(o, 1.0);
+      }
+      for (int j = 0; j < 12; j++)
+        for (int p : fluid) {
+          const double* xp = &x[3 * p];
+          auto nrm = [&](const double* a) {
+            double q = a[0] * a[0];
+            for (int d = 1; d < D; d++) q = q + a[d] * a[d];
+            return std::sqrt(q);
+          };
+          switch (j) {
+            case 0: put<double>(o, xp[0]); break;
+            case 1: put<double>(o, xp[1]); break;
+            case 2: put<double>(o, D == 3 ? xp[2] : 0.0); break;
+            case 3: put<int32_t>(o, phase[p]); break;
+            case 4: put<double>(o, v[3 * p]); break;
+            case 5: put<double>(o, v[3 * p + 1]); break;
+            case 6: put<double>(o, vol[p]); break;
+            case 7: put<double>(o, rho[p]); break;
+            case 8: put<double>(o, P[p]); break;
+            case 9: put<double>(o, nrm(&tv[3 * p])); break;
+            case 10: put<double>(o, nrm(&v[3 * p])); break;
+            default: put<int32_t>(o, (int32_t)nbr[p].size()); break;
+          }
+        }
+      if (!o) return PGDG_EINVAL;
+    }
+    if (cpath) {
+      std::ofstream o(cpath, std::ios::trunc);
+      if (!o) return PGDG_EINVAL;
+      o << "VARIABLES = \"x\",\"y\",\"z\", \"v1\",\"v2\", \"v\",\"rho0\",\"rho1\",        "
+           "\"E0\",\"E1\",\"Lim0\",\"Lim1\",\"st\", \"st1\", \"P\"\n";
+      o << "ZONE T=" << "\"GRID 1\"," << "SOLUTIONTIME=" << st.time << "\n";
+      for (int64_t ci = 0; ci < ncell; ci++) {
+        const double* vc = &cv[3 * ci];
+        double q = vc[0] * vc[0];
+        for (int d = 1; d < D; d++) q = q + vc[d] * vc[d];
+        const double* co = &ccoef[(ci * F + 0) * U * B];
+        o << ccen[3 * ci] << ' ' << ccen[3 * ci + 1] << ' ' << ccen[3 * ci + 2] << ' ' << vc[0] << ' ' << vc[1] << ' '
+          << std::sqrt(q) << ' ' << crho[ci * F + 0] << ' ' << crho[ci * F + 1] << ' ' << co[1 * B + 1] << ' '
+          << co[1 * B + 2] << ' ' << clim[(ci * F + 0) * U] << ' ' << clim[(ci * F + 1) * U] << ' '
+          << calph[ci * F + 0] << ' ' << calph[ci * F + 1] << ' ' << cP[ci] << ' ' << '\n';
+      }
+      if (!o) return PGDG_EINVAL;
+    }
+    return PGDG_OK;
+  }
+
   /* MPM::Output_point (mpm_ini.cpp:774-824): bubble extents along the axis and
    * the phase-2 mass, over particle_fluid in order (the ends start at the
    * box's left and right x) */
@@ -1733,6 +1830,9 @@ int po_set_timestep(po_ctx* ctx, double* dt, double* mv) { return ctx->set_times
 int po_output_point(po_ctx* ctx, double* out5) {
   ctx->output_point(out5);
   return PGDG_OK;
+}
+int po_output_plt(po_ctx* ctx, const char* particle_path, const char* cell_path) {
+  return ctx->output_plt(particle_path, cell_path);
 }
 int po_used_state_update(po_ctx* ctx) { ctx->used_state_update(); return PGDG_OK; }
 int po_bin_particles(po_ctx* ctx) { ctx->bin_particles(); return PGDG_OK; }

@@ -67,6 +67,8 @@ int po_run_step(po_ctx* ctx, int64_t n);     /* MPM_run_simulation */
 int po_advance(po_ctx* ctx, int nsteps);
 int po_totals(po_ctx* ctx, double* out);     /* [F particle mass, particle E, F cell mass, cell E] */
 int po_output_point(po_ctx* ctx, double* out5); /* Output_point: bubble extents, phase-2 mass, count */
+/* Output_plt_file: Tecplot binary of the particles, ASCII table of the cells (either path may be NULL) */
+int po_output_plt(po_ctx* ctx, const char* particle_path, const char* cell_path);
 
 /* batched MGFM with an explicit material table (gamma[m], pinf[m]) */
 int po_mgfm_batched(const double* in6, const int8_t* mat2, const double* gam, const double* pinf,

@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpgdg_gpu.so")
 INC = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# (source, object tag, extra flags): the grid and G2P kernels are compiled twice,
+# (source, object tag, extra flags): the grid, G2P and output kernels are compiled twice,
 # once with FMA contraction (mixed and FP64_FMA paths) and once without
 # (-DPGDG_EXACT_TU: the exact-order FP64 path)
 CU = [("k_particles.cu", "k_particles", ["-fmad=false"]),
@@ -29,8 +29,10 @@ CU = [("k_particles.cu", "k_particles", ["-fmad=false"]),
       ("k_mlp_tc.cu", "k_mlp_tc", []),
       ("k_peak.cu", "k_peak", []),
       ("k_case.cu", "k_case", ["-fmad=false"]),
+      ("k_output.cu", "k_output", []),
+      ("k_output.cu", "k_output_x", ["-fmad=false", "-DPGDG_EXACT_TU"]),
       ("capi.cu", "capi", [])]
-CPP = ["case_builder.cpp"]
+CPP = ["case_builder.cpp", "plt_writer.cpp"]
 
 
 def _nvcc():

@@ -14,10 +14,12 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/pgdg.h"
 #include "pgdg_dev.cuh"
+#include "plt_writer.h"
 
 using namespace pgdg;
 
@@ -40,6 +42,8 @@ struct pgdg_ctx {
   cudaStream_t st = nullptr;
   virtual int upload_particles(const pgdg_particles*) = 0;
   virtual int output_point(double* out5) = 0;
+  virtual int output_plt(const char* particle_path, const char* cell_path, int async) = 0;
+  virtual int output_wait() = 0;
   virtual int case_build(int id, uint64_t seed) = 0;
   virtual int download_particles(pgdg_particles*) = 0;
   virtual int num_particles(int64_t*) = 0;
@@ -158,6 +162,24 @@ struct Ctx : pgdg_ctx {
   bool g2p_partial = false; /* see run_step */
   double *d_gam = nullptr, *d_pinf = nullptr;
   unsigned long long* d_ncell = nullptr;
+  int dev_id = 0;
+  /* the last complete stage's search coordinates and lengths (the flag-2
+   * lists the snapshot writer counts); unset after the particle set changes */
+  int nb_xs = 0, nb_hs = 0;
+  bool nb_set = false;
+  /* snapshot writers: device snapshot, copy stream, pinned chunks, worker */
+  double* d_odv = nullptr;
+  int32_t* d_oiv = nullptr;
+  double* d_odc = nullptr;
+  int64_t ocap = 0;
+  cudaStream_t ost = nullptr;
+  cudaEvent_t oev = nullptr, ochev[2] = {nullptr, nullptr};
+  unsigned char* h_och[2] = {nullptr, nullptr};
+  static constexpr size_t OCHUNK = (size_t)32 << 20;
+  std::thread oth;
+  bool orunning = false;
+  int orc = PGDG_OK;
+  std::string omsg;
 
   template <typename T>
   cudaError_t A(T** p, size_t n) {
@@ -167,6 +189,16 @@ struct Ctx : pgdg_ctx {
   }
 
   ~Ctx() override {
+    output_wait();
+    if (d_odv) cudaFree(d_odv);
+    if (d_oiv) cudaFree(d_oiv);
+    if (d_odc) cudaFree(d_odc);
+    for (int k = 0; k < 2; k++) {
+      if (h_och[k]) cudaFreeHost(h_och[k]);
+      if (ochev[k]) cudaEventDestroy(ochev[k]);
+    }
+    if (oev) cudaEventDestroy(oev);
+    if (ost) cudaStreamDestroy(ost);
     if (st) cudaStreamSynchronize(st);
     drop_graphs();
     for (auto e : ev_pool) cudaEventDestroy(e);
@@ -178,6 +210,7 @@ struct Ctx : pgdg_ctx {
   int init(const pgdg_case* c, int prec, int64_t cap) {
     cs = *c;
     precision = prec;
+    CK(cudaGetDevice(&dev_id));
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     K.dim = D;
     for (int d = 0; d < 3; d++) K.N[d] = (d < D) ? cs.ncell[d] : 1;
@@ -410,6 +443,7 @@ struct Ctx : pgdg_ctx {
   int case_build(int id, uint64_t seed) override {
     drop_graphs();
     fresh_bins = false;
+    nb_set = false;
     const int64_t n = pgdg_case_num_particles(&cs);
     if (n > K.cap) {
       err = "particle count exceeds capacity";
@@ -441,6 +475,7 @@ struct Ctx : pgdg_ctx {
   int upload_particles(const pgdg_particles* pp) override {
     drop_graphs();
     fresh_bins = false;
+    nb_set = false;
     int64_t n = pp->n;
     if (n > K.cap) {
       err = "particle count exceeds capacity";
@@ -812,14 +847,17 @@ struct Ctx : pgdg_ctx {
   int bin() override {
     timed("bin", 2, [&] { Launch<D, R, EX>::bin(K, P, st); });
     fresh_bins = true;
+    nb_set = false;
     return PGDG_OK;
   }
   int split() override {
     timed("split", 14, [&] { Launch<D, R, EX>::split(K, P, st); });
+    nb_set = false;
     return PGDG_OK;
   }
   int merge(bool chained = false) override {
     timed("merge", 14, [&] { Launch<D, R, EX>::merge(K, P, chained, st); });
+    nb_set = false;
     return PGDG_OK;
   }
   /* flag 4: a cell's particle list is its bucket and a particle's in_ele[0]
@@ -961,6 +999,11 @@ struct Ctx : pgdg_ctx {
                      [&](int v) { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, v, pst_scratch, st); });
     timed("pst", 1, [&] { Launch<D, R, EX>::pst(K, P, xs, hs, xn, hn, pst_var, pst_scratch, st); });
     if (md == 1) timed("store_lists", 2, [&] { Launch<D, R, EX>::store_lists(K, P, xs, hs, xn, st); });
+    if (md == 1) {
+      nb_xs = xs;
+      nb_hs = hs;
+      nb_set = true;
+    }
     P.xb = xn;
     P.hb = hn;
     return PGDG_OK;
@@ -1067,6 +1110,10 @@ struct Ctx : pgdg_ctx {
         P.xb = sg.xb_after;
         P.hb = sg.hb_after;
         x0b = sg.x0b_after;
+        /* the graph's last stage searched with the buffers its first stage wrote */
+        nb_xs = 3 - P.xb - x0b;
+        nb_hs = 1 - P.hb;
+        nb_set = true;
         iterate += 3;
         launches += sg.launches;
         s += 3;
@@ -1084,6 +1131,131 @@ struct Ctx : pgdg_ctx {
     Launch<D, R, EX>::probe(K, P, d_tot, d_tot, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaMemcpy(out5, d_tot, 5 * sizeof(double), cudaMemcpyDeviceToHost));
+    return PGDG_OK;
+  }
+  /* ---------------- snapshot writers (Output_plt_file) ----------------
+   * The live particles and the cells are packed on the context stream into a
+   * snapshot that no later call touches; a host thread (or the caller, when
+   * async is 0) then copies it out through two pinned chunks on a copy stream
+   * while it writes the files.  The device goes on with the next steps
+   * meanwhile; a further output call, output_wait() or destruction waits for
+   * the writer. */
+  int output_plt(const char* pp, const char* cp, int async) override {
+    int rc = output_wait();
+    if (rc) return rc;
+    if (!pp && !cp) return PGDG_OK;
+    flush_prof();
+    int64_t n = 0;
+    if (pp) {
+      rc = alive(&n);
+      if (rc) return rc;
+    }
+    const DevCounters hc = counters();
+    if (hc.err) {
+      err = "device status reports an error; no snapshot written";
+      return PGDG_ESTATE;
+    }
+    if (pp && n > ocap) {
+      if (d_odv) cudaFree(d_odv);
+      if (d_oiv) cudaFree(d_oiv);
+      d_odv = nullptr;
+      d_oiv = nullptr;
+      ocap = 0;
+      CK(cudaMalloc(&d_odv, sizeof(double) * 10 * (size_t)std::max<int64_t>(n, 1)));
+      CK(cudaMalloc(&d_oiv, sizeof(int32_t) * 2 * (size_t)std::max<int64_t>(n, 1)));
+      ocap = n;
+    }
+    if (cp && !d_odc) CK(cudaMalloc(&d_odc, sizeof(double) * 12 * (size_t)K.ncell));
+    if (!ost) {
+      CK(cudaStreamCreateWithFlags(&ost, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&oev, cudaEventDisableTiming));
+      for (int k = 0; k < 2; k++) {
+        CK(cudaEventCreateWithFlags(&ochev[k], cudaEventDisableTiming));
+        CK(cudaMallocHost(&h_och[k], OCHUNK));
+      }
+    }
+    const int xs = nb_set ? nb_xs : P.xb, hs = nb_set ? nb_hs : P.hb;
+    if (pp) output_pack_particles<D, R, EX>(K, P, d_alive, n, xs, hs, d_odv, d_oiv, st);
+    if (cp) output_pack_cells<D, R, EX>(K, P, d_odc, st);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(oev, st));
+    const std::string spp = pp ? pp : "", scp = cp ? cp : "";
+    const double time = hc.time;
+    if (async) {
+      orunning = true;
+      oth = std::thread([this, n, time, spp, scp] { orc = output_job(n, time, spp, scp); });
+      return PGDG_OK;
+    }
+    rc = output_job(n, time, spp, scp);
+    if (rc) err = omsg;
+    return rc;
+  }
+  int output_wait() override {
+    if (!orunning) return PGDG_OK;
+    oth.join();
+    orunning = false;
+    const int rc = orc;
+    orc = PGDG_OK;
+    if (rc) err = omsg;
+    return rc;
+  }
+  /* device range -> file through the pinned chunks (the copy of chunk k + 1
+   * overlaps the write of chunk k) */
+  bool copy_out(const void* src, size_t bytes, FILE* f) {
+    const size_t nch = (bytes + OCHUNK - 1) / OCHUNK;
+    auto issue = [&](size_t k) {
+      const size_t off = k * OCHUNK, len = std::min(OCHUNK, bytes - off);
+      cudaMemcpyAsync(h_och[k & 1], static_cast<const char*>(src) + off, len, cudaMemcpyDeviceToHost, ost);
+      cudaEventRecord(ochev[k & 1], ost);
+    };
+    if (nch) issue(0);
+    for (size_t k = 0; k < nch; k++) {
+      if (k + 1 < nch) issue(k + 1);
+      if (cudaEventSynchronize(ochev[k & 1]) != cudaSuccess) return false;
+      const size_t off = k * OCHUNK, len = std::min(OCHUNK, bytes - off);
+      if (std::fwrite(h_och[k & 1], 1, len, f) != len) return false;
+    }
+    return true;
+  }
+  int output_job(int64_t n, double time, const std::string& pp, const std::string& cp) {
+    if (cudaSetDevice(dev_id) != cudaSuccess || cudaStreamWaitEvent(ost, oev, 0) != cudaSuccess) {
+      omsg = "snapshot writer: CUDA setup failed";
+      return PGDG_ECUDA;
+    }
+    if (!pp.empty()) {
+      FILE* f = std::fopen(pp.c_str(), "wb");
+      if (!f) {
+        omsg = "cannot open " + pp;
+        return PGDG_EINVAL;
+      }
+      const std::string hdr = pgdg_out::plt_header(n, time);
+      bool ok = std::fwrite(hdr.data(), 1, hdr.size(), f) == hdr.size();
+      /* file order x y z phase vx vy vol rho P tv v n_neighbor: (int32?, index) */
+      static const int kind[12] = {0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1};
+      static const int idx[12] = {0, 1, 2, 0, 3, 4, 5, 6, 7, 8, 9, 1};
+      for (int j = 0; j < 12 && ok; j++) {
+        if (kind[j] == 0) ok = copy_out(d_odv + (size_t)idx[j] * n, sizeof(double) * (size_t)n, f);
+        else ok = copy_out(d_oiv + (size_t)idx[j] * n, sizeof(int32_t) * (size_t)n, f);
+      }
+      if (std::fclose(f) != 0) ok = false;
+      if (!ok) {
+        omsg = "writing " + pp + " failed";
+        return PGDG_ECUDA;
+      }
+    }
+    if (!cp.empty()) {
+      std::vector<double> cols(12 * (size_t)K.ncell);
+      if (cudaMemcpyAsync(cols.data(), d_odc, sizeof(double) * cols.size(), cudaMemcpyDeviceToHost, ost) !=
+              cudaSuccess ||
+          cudaStreamSynchronize(ost) != cudaSuccess) {
+        omsg = "snapshot writer: cell copy failed";
+        return PGDG_ECUDA;
+      }
+      const unsigned hw = std::thread::hardware_concurrency();
+      if (pgdg_out::write_cell_table(cp.c_str(), D, K.N, cs.box_l, cs.p_size, cols.data(), time,
+                                     (int)std::max(1u, std::min(hw, 16u)), &omsg))
+        return PGDG_EINVAL;
+    }
     return PGDG_OK;
   }
   int totals(double* out) override {
@@ -1150,6 +1322,14 @@ int pgdg_upload_particles(pgdg_ctx* ctx, const pgdg_particles* p) { return ctx->
 int pgdg_output_point(pgdg_ctx* ctx, double* out5) {
   if (!ctx || !out5) return PGDG_EINVAL;
   return ctx->output_point(out5);
+}
+int pgdg_output_plt(pgdg_ctx* ctx, const char* particle_path, const char* cell_path, int async) {
+  if (!ctx) return PGDG_EINVAL;
+  return ctx->output_plt(particle_path, cell_path, async);
+}
+int pgdg_output_wait(pgdg_ctx* ctx) {
+  if (!ctx) return PGDG_EINVAL;
+  return ctx->output_wait();
 }
 int pgdg_case_build(pgdg_ctx* ctx, int config_id, uint64_t seed) {
   if (!ctx || config_id < 1 || config_id > 4) return PGDG_EINVAL;

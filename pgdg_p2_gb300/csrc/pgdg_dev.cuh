@@ -306,6 +306,16 @@ template <int D, typename R>
 int case_build(const CaseK& K, const DevPtrs<R>& P, const pgdg_case& cs, int id, uint64_t seed, int64_t n,
                cudaStream_t st);
 
+/* snapshot packing of Output_plt_file (k_output.cu): the n live particles of
+ * alive[] into dv (10 x n doubles: x y z vx vy vol rho P |tv| |v|) and iv
+ * (2 x n int32: phase, flag-2 list size over coordinates X[xs] and lengths
+ * H[hs]); the cells into dc (12 doubles per cell) */
+template <int D, typename R, bool EX>
+void output_pack_particles(const CaseK& K, const DevPtrs<R>& P, const int64_t* alive, int64_t n, int xs, int hs,
+                           double* dv, int32_t* iv, cudaStream_t st);
+template <int D, typename R, bool EX>
+void output_pack_cells(const CaseK& K, const DevPtrs<R>& P, double* dc, cudaStream_t st);
+
 /* minimum resident 128-thread blocks per SM asked of the FP32 instantiations of
  * the per-cell and per-particle kernels (a register cap that trades a few
  * registers for more warps in flight; these kernels are latency-bound); the

@@ -60,6 +60,8 @@ def lib():
         L.pgdg_totals.argtypes = [vp, P(C.c_double)]
         L.pgdg_output_point.argtypes = [vp, P(C.c_double)]
         L.pgdg_case_build.argtypes = [vp, C.c_int, C.c_uint64]
+        L.pgdg_output_plt.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int]
+        L.pgdg_output_wait.argtypes = [vp]
         L.pgdg_profile.argtypes = [vp, C.c_int]
         L.pgdg_profile_read.argtypes = [vp, C.c_char_p, C.c_int, P(C.c_double), P(C.c_int64), C.c_int, P(C.c_int)]
         L.pgdg_launch_count.argtypes = [vp, P(C.c_int64)]
@@ -260,6 +262,17 @@ class MPM:
         out = np.zeros(5)
         self._ck(lib().pgdg_output_point(self.h, out.ctypes.data_as(C.POINTER(C.c_double))), "output_point")
         return out
+
+    def output_plt(self, particle_path=None, cell_path=None, async_write=False):
+        """Output_plt_file: the particle Tecplot binary and the cell table.  With
+        async_write the call returns once the snapshot is packed on the device;
+        output_wait() joins the writer."""
+        enc = (lambda p: str(p).encode() if p is not None else None)
+        self._ck(lib().pgdg_output_plt(self.h, enc(particle_path), enc(cell_path), 1 if async_write else 0),
+                 "output_plt")
+
+    def output_wait(self):
+        self._ck(lib().pgdg_output_wait(self.h), "output_wait")
 
     def totals(self):
         out = np.zeros(6)

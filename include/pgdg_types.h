@@ -16,7 +16,7 @@
 extern "C" {
 #endif
 
-#define PGDG_MAX_FLD 2          /* FldNum (glbparam.h:41) */
+#define PGDG_MAX_FLD 3          /* the largest FldNum of a build (glbparam.h:41: 2; Triple_point_3phase: 3) */
 #define PGDG_PHASE_BOUNDARY 10  /* boundary particle phase (mpm_ini.cpp:586) */
 
 /* error codes returned by every entry point */
@@ -56,7 +56,7 @@ enum { PGDG_MGFM_3D = 0, PGDG_MGFM_2D = 1 };
  * particle_flow.cpp:332-339). */
 typedef struct pgdg_case {
   int32_t dim;            /* 2 or 3 */
-  int32_t nfld;           /* number of materials, 2 */
+  int32_t nfld;           /* number of materials: 2, or 3 (the three-material build) */
   int32_t ncell[3];       /* NUM (cells per axis; 1 for z in 2D) */
   int32_t bc[6];          /* boundary kind per side: xL, xR, yL, yR, zL, zR */
   int32_t mgfm_variant;   /* PGDG_MGFM_3D or PGDG_MGFM_2D */

@@ -18,14 +18,14 @@ from pgdg_p2_gb300.abi import (Cells, Particles, check, pgdg_case, pgdg_cells,  
                                pgdg_particles, pgdg_stats)
 from oracle import build as _build  # noqa: E402
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = _build.build()
-        L = C.CDLL(path)
+def lib(nfld=2):
+    """The oracle library of a material count (2, or 3 for the three-material case)."""
+    if nfld not in _libs:
+        _build.build()
+        L = C.CDLL(_build.lib_path(nfld))
         P = C.POINTER
         vp = C.c_void_p
         L.po_create.argtypes = [P(pgdg_case), P(vp)]
@@ -63,8 +63,8 @@ def lib():
         L.po_case_num_particles.restype = C.c_int64
         L.po_case_particles.argtypes = [P(pgdg_case), C.c_int, C.c_uint64, P(pgdg_particles)]
         L.po_case_cells.argtypes = [P(pgdg_case), P(pgdg_cells)]
-        _lib = L
-    return _lib
+        _libs[nfld] = L
+    return _libs[nfld]
 
 
 def set_threads(n):
@@ -86,7 +86,7 @@ def case_particles(cs, config_id, seed=0):
 
 
 def case_cells(cs):
-    c = Cells(cs.ncells, cs.dim)
+    c = Cells(cs.ncells, cs.dim, nfld=cs.nfld)
     check(lib().po_case_cells(C.byref(cs), C.byref(c.view())), "po_case_cells")
     return c
 
@@ -104,37 +104,38 @@ class Oracle:
         self.cs = cs
         self.dim = cs.dim
         self.h = C.c_void_p()
-        check(lib().po_create(C.byref(cs), C.byref(self.h)), "po_create")
+        self._L = lib(cs.nfld)
+        check(self._L.po_create(C.byref(cs), C.byref(self.h)), "po_create")
 
     def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
-            _lib.po_destroy(self.h)
+        if getattr(self, "h", None) and getattr(self, "_L", None) is not None:
+            self._L.po_destroy(self.h)
             self.h = None
 
     # ---- state exchange ----
     def upload_particles(self, p: Particles):
         v = p.view()
         v.n = p.n
-        check(lib().po_upload_particles(self.h, C.byref(v)), "upload_particles")
+        check(self._L.po_upload_particles(self.h, C.byref(v)), "upload_particles")
 
     def num_particles(self):
         n = C.c_int64()
-        lib().po_num_particles(self.h, C.byref(n))
+        self._L.po_num_particles(self.h, C.byref(n))
         return n.value
 
     def download_particles(self):
         n = self.num_particles()
         p = Particles(n, self.dim)
         v = p.view()
-        check(lib().po_download_particles(self.h, C.byref(v)), "download_particles")
+        check(self._L.po_download_particles(self.h, C.byref(v)), "download_particles")
         return p
 
     def upload_cells(self, c: Cells):
-        check(lib().po_upload_cells(self.h, C.byref(c.view())), "upload_cells")
+        check(self._L.po_upload_cells(self.h, C.byref(c.view())), "upload_cells")
 
     def download_cells(self):
-        c = Cells(self.cs.ncells, self.dim)
-        check(lib().po_download_cells(self.h, C.byref(c.view())), "download_cells")
+        c = Cells(self.cs.ncells, self.dim, nfld=self.cs.nfld)
+        check(self._L.po_download_cells(self.h, C.byref(c.view())), "download_cells")
         return c
 
     def _csr(self, fn, nrow):
@@ -147,91 +148,92 @@ class Oracle:
         return off, ent[: tot.value]
 
     def download_lists(self):
-        return self._csr(lib().po_download_lists, self.num_particles())
+        return self._csr(self._L.po_download_lists, self.num_particles())
 
     def download_cell_lists(self):
-        return self._csr(lib().po_download_cell_lists, self.cs.ncells)
+        return self._csr(self._L.po_download_cell_lists, self.cs.ncells)
 
     def upload_lists(self, off, ent):
         off = np.ascontiguousarray(off, np.int64)
         ent = np.ascontiguousarray(ent if len(ent) else np.zeros(1, np.int64), np.int64)
-        check(lib().po_upload_lists(self.h, off.ctypes.data_as(C.POINTER(C.c_int64)),
+        check(self._L.po_upload_lists(self.h, off.ctypes.data_as(C.POINTER(C.c_int64)),
                                     ent.ctypes.data_as(C.POINTER(C.c_int64))), "upload_lists")
 
     def set_dt(self, dt):
-        lib().po_set_dt(self.h, float(dt))
+        self._L.po_set_dt(self.h, float(dt))
 
     def set_iterate(self, n):
-        lib().po_set_iterate(self.h, int(n))
+        self._L.po_set_iterate(self.h, int(n))
 
     def set_max_v(self, mv):
-        lib().po_set_max_v(self.h, float(mv))
+        self._L.po_set_max_v(self.h, float(mv))
 
     def stats(self):
         s = pgdg_stats()
-        lib().po_get_stats(self.h, C.byref(s))
+        self._L.po_get_stats(self.h, C.byref(s))
         return s.to_dict()
 
     # ---- reference methods ----
     def Set_timestep(self):
         dt, mv = C.c_double(), C.c_double()
-        lib().po_set_timestep(self.h, C.byref(dt), C.byref(mv))
+        self._L.po_set_timestep(self.h, C.byref(dt), C.byref(mv))
         return dt.value, mv.value
 
     def Used_state_update(self):
-        lib().po_used_state_update(self.h)
+        self._L.po_used_state_update(self.h)
 
     def Map_the_particle_to_tree(self):
-        lib().po_bin_particles(self.h)
+        self._L.po_bin_particles(self.h)
 
     def Split_particle_fast(self):
-        lib().po_split_particle_fast(self.h)
+        self._L.po_split_particle_fast(self.h)
 
     def Merge_particle_fast(self):
-        lib().po_merge_particle_fast(self.h)
+        self._L.po_merge_particle_fast(self.h)
 
     def Refresh_membership(self):
-        lib().po_refresh_membership(self.h)
+        self._L.po_refresh_membership(self.h)
 
     def Refresh_neighbors(self):
-        lib().po_refresh_neighbors(self.h)
+        self._L.po_refresh_neighbors(self.h)
 
     def MLS_P2G(self):
-        lib().po_mls_p2g(self.h)
+        self._L.po_mls_p2g(self.h)
 
     def Calculate_limiter(self):
-        lib().po_calculate_limiter(self.h)
+        self._L.po_calculate_limiter(self.h)
 
     def Grid_acceleration(self):
-        lib().po_grid_acceleration(self.h)
+        self._L.po_grid_acceleration(self.h)
 
     def Update_grid(self, md):
-        lib().po_update_grid(self.h, int(md))
+        self._L.po_update_grid(self.h, int(md))
 
     def Update_particle(self, md):
-        lib().po_update_particle(self.h, int(md))
+        self._L.po_update_particle(self.h, int(md))
 
     def MPM_run_simulation(self, n):
-        lib().po_run_step(self.h, int(n))
+        self._L.po_run_step(self.h, int(n))
 
     def advance(self, nsteps):
-        lib().po_advance(self.h, int(nsteps))
+        self._L.po_advance(self.h, int(nsteps))
 
     def output_point(self):
         out = np.zeros(5)
-        lib().po_output_point(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        self._L.po_output_point(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
     def output_plt(self, particle_path=None, cell_path=None):
         """Output_plt_file: the particle Tecplot binary and the cell table."""
         enc = (lambda p: str(p).encode() if p is not None else None)
-        rc = lib().po_output_plt(self.h, enc(particle_path), enc(cell_path))
+        rc = self._L.po_output_plt(self.h, enc(particle_path), enc(cell_path))
         if rc != 0:
             raise RuntimeError(f"po_output_plt failed ({rc})")
 
     def totals(self):
-        out = np.zeros(6)
-        lib().po_totals(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        """Particle mass per phase, particle energy, cell mass per phase, cell energy."""
+        out = np.zeros(2 * self.cs.nfld + 2)
+        self._L.po_totals(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
 

@@ -65,6 +65,11 @@ State initial_state(int id, const double x[3], int dim) {
     if (x[0] < 1.0) return {1, 1.0, 1.0, 0.0};
     return x[1] < 1.5 ? State{1, 1.0, 0.1, 0.0} : State{2, 0.125, 0.1, 0.0};
   }
+  if (id == 5) {
+    /* Triple_point_3phase/mpm_ini.cpp:157-245: f1 = x > 1 and y < 1.5 */
+    if (x[0] > 1.0 && x[1] < 1.5) return {1, 1.0, 0.1, 0.0};
+    return x[0] > 1.0 ? State{2, 0.125, 0.1, 0.0} : State{3, 1.0, 1.0, 0.0};
+  }
   if (id == 4) {
     const double r2 = x[0] * x[0] + x[1] * x[1];
     return r2 < 0.3 * 0.3 ? State{2, 1270.0, 8.29e8, 0.0} : State{1, 1000.0, 1e5, 0.0};
@@ -90,26 +95,32 @@ int lattice_count(const pgdg_case* cs, int d) {
 extern "C" {
 
 int po_case_setup(int id, const int32_t* ncell, pgdg_case* cs) {
-  if (!cs || id < 1 || id > 4) return PGDG_EINVAL;
+  if (!cs || id < 1 || id > 5) return PGDG_EINVAL;
   std::memset(cs, 0, sizeof(*cs));
   struct Workload {
     int dim, n[3];
     double lo[3], hi[3];
-    double gam[2], pinf[2], rho0[2];
+    int nfld;
+    double gam[3], pinf[3], rho0[3];
     int bc[6];
     int mgfm;
   };
   const int W = PGDG_BC_WALL, I = PGDG_BC_INLET, O = PGDG_BC_OUTLET, S = PGDG_BC_SYMMETRY,
             T = PGDG_BC_TRANSMISSIVE;
-  static const Workload table[4] = {
-      {2, {112, 48, 1}, {0, 0, 0}, {7, 3, 0}, {1.5, 1.4}, {0, 0}, {1.0, 0.125}, {W, W, W, W, 0, 0}, PGDG_MGFM_2D},
-      {3, {256, 64, 64}, {0, 0, 0}, {4, 1, 1}, {1.4, 1.648}, {0, 0}, {1.0, 0.138}, {I, O, S, W, S, S}, PGDG_MGFM_3D},
-      {3, {384, 96, 96}, {0, 0, 0}, {4, 1, 1}, {1.4, 1.648}, {0, 0}, {1.0, 0.138}, {I, O, S, W, S, W}, PGDG_MGFM_3D},
-      {2, {1024, 1024, 1}, {-1, -1, 0}, {1, 1, 0}, {7.15, 2.0}, {3.309e8, 0}, {1000.0, 1270.0}, {T, T, T, T, 0, 0},
-       PGDG_MGFM_2D}};
+  static const Workload table[5] = {
+      {2, {112, 48, 1}, {0, 0, 0}, {7, 3, 0}, 2, {1.5, 1.4}, {0, 0}, {1.0, 0.125}, {W, W, W, W, 0, 0}, PGDG_MGFM_2D},
+      {3, {256, 64, 64}, {0, 0, 0}, {4, 1, 1}, 2, {1.4, 1.648}, {0, 0}, {1.0, 0.138}, {I, O, S, W, S, S},
+       PGDG_MGFM_3D},
+      {3, {384, 96, 96}, {0, 0, 0}, {4, 1, 1}, 2, {1.4, 1.648}, {0, 0}, {1.0, 0.138}, {I, O, S, W, S, W},
+       PGDG_MGFM_3D},
+      {2, {1024, 1024, 1}, {-1, -1, 0}, {1, 1, 0}, 2, {7.15, 2.0}, {3.309e8, 0}, {1000.0, 1270.0},
+       {T, T, T, T, 0, 0}, PGDG_MGFM_2D},
+      /* Triple_point_3phase/mpm_ini.cpp:80-97 materials on C1's box */
+      {2, {112, 48, 1}, {0, 0, 0}, {7, 3, 0}, 3, {1.4, 1.5, 1.6}, {0, 0, 0.1}, {1.0, 0.125, 0.125},
+       {W, W, W, W, 0, 0}, PGDG_MGFM_2D}};
   const Workload& w = table[id - 1];
   cs->dim = w.dim;
-  cs->nfld = 2;
+  cs->nfld = w.nfld;
   cs->merge_iters = 4; /* mpm_ini.cpp:708 */
   cs->cfl = 0.3;       /* particle.cpp:558 */
   cs->mgfm_variant = w.mgfm;
@@ -120,7 +131,7 @@ int po_case_setup(int id, const int32_t* ncell, pgdg_case* cs) {
     cs->ncell[d] = d < w.dim ? ((ncell && ncell[d] > 0) ? ncell[d] : w.n[d]) : 1;
     cs->p_size[d] = d < w.dim ? (w.hi[d] - w.lo[d]) / (double)cs->ncell[d] : 0.0;
   }
-  for (int s = 0; s < 2; s++) {
+  for (int s = 0; s < w.nfld; s++) {
     cs->gamma[s] = w.gam[s];
     cs->pinf[s] = w.pinf[s];
     cs->ini_rho[s] = w.rho0[s];
@@ -160,7 +171,7 @@ int po_case_particles(const pgdg_case* cs, int id, uint64_t seed, pgdg_particles
   const int D = cs->dim, NS = (D + 2) * D;
   const int ni = lattice_count(cs, 0), nj = lattice_count(cs, 1), nk = lattice_count(cs, 2);
   Mix64 rng{seed ? seed : 20260101ull};
-  const double jitter = id == 1 ? cs->p_g / 8.0 : 0.0;
+  const double jitter = (id == 1 || id == 5) ? cs->p_g / 8.0 : 0.0;
   double vol = 1;
   for (int d = 0; d < D; d++) vol *= cs->p_sz; /* powern(p_sz, DIM) */
   const double ini_h = 3.2 / 2. * cs->p_sz;     /* CELL_RATIO / CUT_OFF * p_sz */
@@ -205,7 +216,7 @@ int po_case_particles(const pgdg_case* cs, int id, uint64_t seed, pgdg_particles
 
 int po_case_cells(const pgdg_case* cs, pgdg_cells* c) {
   if (!cs || !c) return PGDG_EINVAL;
-  const int D = cs->dim, U = D + 2, B = D + 1, F = 2;
+  const int D = cs->dim, U = D + 2, B = D + 1, F = cs->nfld;
   const int64_t n = (int64_t)cs->ncell[0] * cs->ncell[1] * (D == 3 ? cs->ncell[2] : 1);
   if (c->n != n) return PGDG_EINVAL;
   for (int64_t ci = 0; ci < n; ci++) {

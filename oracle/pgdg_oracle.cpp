@@ -32,6 +32,10 @@
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
+
+#ifndef PO_NFLD
+#define PO_NFLD 2
+#endif
 #endif
 
 using namespace oracle;
@@ -77,7 +81,7 @@ struct Face {
 
 template <int D>
 struct OracleT : po_ctx {
-  static constexpr int F = 2;
+  static constexpr int F = PO_NFLD; /* FldNum (glbparam.h:41), fixed per build */
   static constexpr int U = D + 2;
   static constexpr int B = D + 1;
   static constexpr int NS = U * D;  /* stored slopes per particle */
@@ -1496,8 +1500,11 @@ struct OracleT : po_ctx {
         cm[s].add(voli * calph[ci * F + s] * crho[ci * F + s]);
         ce.add(voli * calph[ci * F + s] * cE[ci * F + s]);
       }
-    out[0] = pm[0].value(); out[1] = pm[1].value(); out[2] = pe.value();
-    out[3] = cm[0].value(); out[4] = cm[1].value(); out[5] = ce.value();
+    /* per phase particle masses, particle energy, per phase cell masses, cell energy */
+    for (int s = 0; s < F; s++) out[s] = pm[s].value();
+    out[F] = pe.value();
+    for (int s = 0; s < F; s++) out[F + 1 + s] = cm[s].value();
+    out[2 * F + 1] = ce.value();
   }
   /* MPM::Output_plt_file (mpm_ini.cpp:832-980): the particles as a Tecplot
    * binary (#!TDV112, one ordered zone, twelve variables stored one after the
@@ -1788,7 +1795,7 @@ extern "C" {
 
 int po_create(const pgdg_case* cs, po_ctx** out) {
   if (!cs || !out) return PGDG_EINVAL;
-  if (cs->nfld != 2) return PGDG_EINVAL;
+  if (cs->nfld != PO_NFLD) return PGDG_EINVAL; /* one material count per build */
   if (cs->dim == 2) *out = new OracleT<2>(cs);
   else if (cs->dim == 3) *out = new OracleT<3>(cs);
   else return PGDG_EINVAL;

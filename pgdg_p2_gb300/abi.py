@@ -17,7 +17,8 @@ ERRORS = {
 BC_INTERIOR, BC_WALL, BC_INLET, BC_OUTLET, BC_SYMMETRY, BC_TRANSMISSIVE = 0, 1, -1, -2, -3, -4
 MGFM_3D, MGFM_2D = 0, 1
 PREC_FP64, PREC_MIXED, PREC_FP64_FMA = 0, 1, 2
-F = 2
+F = 2            # materials of the default build
+MAX_FLD = 3      # PGDG_MAX_FLD: the largest material count of a build
 
 
 class PgdgError(RuntimeError):
@@ -37,8 +38,8 @@ class pgdg_case(C.Structure):
         ("mgfm_variant", C.c_int32), ("merge_iters", C.c_int32),
         ("box_l", C.c_double * 3), ("box_r", C.c_double * 3), ("p_size", C.c_double * 3),
         ("p_g", C.c_double), ("p_sz", C.c_double),
-        ("gamma", C.c_double * 2), ("pinf", C.c_double * 2), ("ini_rho", C.c_double * 2),
-        ("c_ini", C.c_double * 2), ("inlet_rho", C.c_double), ("inlet_u", C.c_double * 3),
+        ("gamma", C.c_double * MAX_FLD), ("pinf", C.c_double * MAX_FLD), ("ini_rho", C.c_double * MAX_FLD),
+        ("c_ini", C.c_double * MAX_FLD), ("inlet_rho", C.c_double), ("inlet_u", C.c_double * 3),
         ("inlet_p", C.c_double), ("cfl", C.c_double), ("probe", (C.c_double * 3) * 8),
     ]
 
@@ -181,27 +182,28 @@ class Cells:
     NAMES = ("rho", "rhov", "E", "c", "ac", "alph", "coef", "v", "P", "ph_state", "ph_state_b",
              "used", "lim_u", "g_v", "dcoef")
 
-    def __init__(self, n, dim, alloc=None):
+    def __init__(self, n, dim, alloc=None, nfld=F):
         z = alloc or np.zeros
         self.dim = dim
         self.n = int(n)
+        self.nfld = nf = int(nfld)
         U, B = dim + 2, dim + 1
         f8 = np.float64
-        self.rho = z((n, F), f8)
-        self.rhov = z((n, F, 3), f8)
-        self.E = z((n, F), f8)
-        self.c = z((n, F), f8)
-        self.ac = z((n, F), f8)
-        self.alph = z((n, F), f8)
-        self.coef = z((n, F, U, B), f8)
+        self.rho = z((n, nf), f8)
+        self.rhov = z((n, nf, 3), f8)
+        self.E = z((n, nf), f8)
+        self.c = z((n, nf), f8)
+        self.ac = z((n, nf), f8)
+        self.alph = z((n, nf), f8)
+        self.coef = z((n, nf, U, B), f8)
         self.v = z((n, 3), f8)
         self.P = z((n,), f8)
-        self.ph_state = z((n, F), np.int32)
-        self.ph_state_b = z((n, F), np.int32)
+        self.ph_state = z((n, nf), np.int32)
+        self.ph_state_b = z((n, nf), np.int32)
         self.used = z((n,), np.int32)
-        self.lim_u = z((n, F, U), f8)
+        self.lim_u = z((n, nf, U), f8)
         self.g_v = z((n, dim, dim), f8)
-        self.dcoef = z((n, F, U, B), f8)
+        self.dcoef = z((n, nf, U, B), f8)
 
     def view(self):
         s = pgdg_cells()
@@ -213,7 +215,7 @@ class Cells:
         return s
 
     def copy(self):
-        o = Cells(self.n, self.dim)
+        o = Cells(self.n, self.dim, nfld=self.nfld)
         for k in self.NAMES:
             setattr(o, k, getattr(self, k).copy())
         return o

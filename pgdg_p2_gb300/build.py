@@ -1,7 +1,9 @@
 """Build of libpgdg_gpu.so for sm_103a (in tree, nvcc only, no cmake).
 
 Each CUDA translation unit is compiled in parallel to an object, then linked into
-pgdg_p2_gb300/_build/libpgdg_gpu.so.  k_particles.cu (split/merge/binning) is
+pgdg_p2_gb300/_build/libpgdg_gpu.so (two materials) and, from the same sources
+with -DPGDG_NFLD=3, pgdg_p2_gb300/_build_f3/libpgdg_gpu_f3.so (the 2D
+three-material instance; FldNum is a compile-time constant, as in the reference).  k_particles.cu (split/merge/binning) is
 compiled with -fmad=false so its FP64 arithmetic matches the oracle bit for bit.
 """
 import concurrent.futures as cf
@@ -51,24 +53,42 @@ def _deps():
     return d
 
 
+def lib_path(nfld=2):
+    """The library of a material count: libpgdg_gpu.so (two materials, every 2D and
+    3D workload) or libpgdg_gpu_f3.so (-DPGDG_NFLD=3, the 2D three-material case)."""
+    return LIB if nfld == 2 else os.path.join(HERE, f"_build_f{nfld}", f"libpgdg_gpu_f{nfld}.so")
+
+
 def build(force=False, verbose=False):
-    os.makedirs(OUT, exist_ok=True)
-    if not force and os.path.exists(LIB):
-        t = os.path.getmtime(LIB)
-        if all(os.path.getmtime(x) <= t for x in _deps()):
-            return LIB
+    """Builds both libraries (their translation units compiled in parallel);
+    returns the two-material library's path."""
     nvcc = _nvcc()
-    jobs = []
-    for f, tag, extra in CU:
-        obj = os.path.join(OUT, tag + ".o")
-        cmd = [nvcc] + ARCH + extra + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                                       "-I", INC, "-c", os.path.join(CSRC, f), "-o", obj]
-        jobs.append((cmd, obj))
-    for f in CPP:
-        obj = os.path.join(OUT, f + ".o")
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INC, "-c",
-               os.path.join(CSRC, f), "-o", obj]
-        jobs.append((cmd, obj))
+    deps = _deps()
+    jobs, links = [], []
+    for nfld in (2, 3):
+        lib = lib_path(nfld)
+        out = os.path.dirname(lib)
+        os.makedirs(out, exist_ok=True)
+        if not force and os.path.exists(lib):
+            t = os.path.getmtime(lib)
+            if all(os.path.getmtime(x) <= t for x in deps):
+                continue
+        nf = [] if nfld == 2 else [f"-DPGDG_NFLD={nfld}"]
+        objs = []
+        for f, tag, extra in CU:
+            obj = os.path.join(out, tag + ".o")
+            cmd = [nvcc] + ARCH + extra + nf + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler",
+                                                "-fPIC,-ffp-contract=off", "-I", INC, "-c",
+                                                os.path.join(CSRC, f), "-o", obj]
+            jobs.append((cmd, obj))
+            objs.append(obj)
+        for f in CPP:
+            obj = os.path.join(out, f + ".o")
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INC, "-c",
+                   os.path.join(CSRC, f), "-o", obj]
+            jobs.append((cmd, obj))
+            objs.append(obj)
+        links.append((lib, objs))
 
     def run(job):
         cmd, obj = job
@@ -79,14 +99,17 @@ def build(force=False, verbose=False):
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(run, jobs))
-    tmp = LIB + ".tmp"
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            list(ex.map(run, jobs))
+    for lib, objs in links:
+        tmp = lib + ".tmp"
+        # every symbol resolved at link time (a missing instantiation fails here, not at load)
+        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-Xlinker", "--no-undefined"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, lib)
     return LIB
 
 

@@ -1261,7 +1261,7 @@ struct Ctx : pgdg_ctx {
   int totals(double* out) override {
     Launch<D, R, EX>::totals(K, P, d_tot, st);
     CK(cudaStreamSynchronize(st));
-    CK(cudaMemcpy(out, d_tot, 6 * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out, d_tot, (2 * F + 2) * sizeof(double), cudaMemcpyDeviceToHost));
     return PGDG_OK;
   }
 };
@@ -1272,7 +1272,12 @@ struct Ctx : pgdg_ctx {
 extern "C" {
 
 int pgdg_create(const pgdg_case* cs, int precision, int64_t capacity, pgdg_ctx** out) {
-  if (!cs || !out || cs->nfld != 2 || (cs->dim != 2 && cs->dim != 3)) return PGDG_EINVAL;
+  if (!cs || !out || (cs->dim != 2 && cs->dim != 3)) return PGDG_EINVAL;
+  if (cs->nfld != F) {
+    fprintf(stderr, "pgdg_create: the case has %d materials; this build holds %d (FldNum is fixed per build)\n",
+            cs->nfld, F);
+    return PGDG_EINVAL;
+  }
   if (precision != PGDG_PREC_FP64 && precision != PGDG_PREC_MIXED && precision != PGDG_PREC_FP64_FMA)
     return PGDG_EINVAL;
   for (int d = 0; d < cs->dim; d++)
@@ -1299,9 +1304,14 @@ int pgdg_create(const pgdg_case* cs, int precision, int64_t capacity, pgdg_ctx**
     else if (precision == PGDG_PREC_FP64_FMA) PGDG_MK(2, double, false)
     else PGDG_MK(2, float, false)
   } else {
+#if PGDG_WITH_3D
     if (precision == PGDG_PREC_FP64) PGDG_MK(3, double, true)
     else if (precision == PGDG_PREC_FP64_FMA) PGDG_MK(3, double, false)
     else PGDG_MK(3, float, false)
+#else
+    fprintf(stderr, "pgdg_create: this build holds the 2D three-material instance only\n");
+    return PGDG_EINVAL;
+#endif
   }
 #undef PGDG_MK
   if (rc) {
@@ -1332,7 +1342,7 @@ int pgdg_output_wait(pgdg_ctx* ctx) {
   return ctx->output_wait();
 }
 int pgdg_case_build(pgdg_ctx* ctx, int config_id, uint64_t seed) {
-  if (!ctx || config_id < 1 || config_id > 4) return PGDG_EINVAL;
+  if (!ctx || config_id < 1 || config_id > 5) return PGDG_EINVAL;
   return ctx->case_build(config_id, seed);
 }
 int pgdg_download_particles(pgdg_ctx* ctx, pgdg_particles* p) { return ctx->download_particles(p); }

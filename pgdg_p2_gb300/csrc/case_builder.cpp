@@ -45,7 +45,7 @@ int npart_axis(const pgdg_case* cs, int d) {
 extern "C" {
 
 int pgdg_case_setup(int id, const int32_t* ncell, pgdg_case* cs) {
-  if (!cs || id < 1 || id > 4) return PGDG_EINVAL;
+  if (!cs || id < 1 || id > 5) return PGDG_EINVAL;
   std::memset(cs, 0, sizeof(*cs));
   cs->nfld = 2;
   cs->merge_iters = 4;
@@ -75,6 +75,18 @@ int pgdg_case_setup(int id, const int32_t* ncell, pgdg_case* cs) {
       cs->mgfm_variant = PGDG_MGFM_3D;
       post_shock(cs->inlet_rho, cs->inlet_u[0], cs->inlet_p);
       break;
+    case 5:
+      /* the triple point with three materials (Triple_point_3phase/mpm_ini.cpp:
+       * 80-97): C1's box, cells, walls and sub-lattice */
+      cs->dim = 2; def[0] = 112; def[1] = 48; def[2] = 1;
+      cs->nfld = 3;
+      cs->box_l[0] = 0; cs->box_l[1] = 0; cs->box_r[0] = 7; cs->box_r[1] = 3;
+      cs->gamma[0] = 1.4; cs->pinf[0] = 0; cs->ini_rho[0] = 1.0;
+      cs->gamma[1] = 1.5; cs->pinf[1] = 0; cs->ini_rho[1] = 0.125;
+      cs->gamma[2] = 1.6; cs->pinf[2] = 0.1; cs->ini_rho[2] = 0.125;
+      for (int s = 0; s < 4; s++) cs->bc[s] = PGDG_BC_WALL;
+      cs->mgfm_variant = PGDG_MGFM_2D;
+      break;
     default:
       cs->dim = 2; def[0] = 1024; def[1] = 1024; def[2] = 1;
       cs->box_l[0] = -1; cs->box_l[1] = -1; cs->box_r[0] = 1; cs->box_r[1] = 1;
@@ -95,7 +107,7 @@ int pgdg_case_setup(int id, const int32_t* ncell, pgdg_case* cs) {
   if (cs->dim == 3) prod = prod * cs->p_size[2];
   double root = (cs->dim == 2) ? std::sqrt(prod) : std::cbrt(prod);
   cs->p_sz = root / std::round(cs->p_g / (cs->p_g / 2.0));
-  for (int s = 0; s < 2; s++) cs->c_ini[s] = std::sqrt(cs->gamma[s] * (cs->pinf[s] + 0) / cs->ini_rho[s]);
+  for (int s = 0; s < cs->nfld; s++) cs->c_ini[s] = std::sqrt(cs->gamma[s] * (cs->pinf[s] + 0) / cs->ini_rho[s]);
   /* positivity probe points (mpm.cpp:694-706) */
   int k = 0;
   for (int jj = 0; jj < 4; jj++) {
@@ -122,7 +134,7 @@ int pgdg_case_particles(const pgdg_case* cs, int id, uint64_t seed, pgdg_particl
   const int NS = U * D;
   int na[3] = {npart_axis(cs, 0), npart_axis(cs, 1), npart_axis(cs, 2)};
   const uint64_t rs = seed ? seed : 20260101ull;
-  const double jit = (id == 1) ? cs->p_g / 8.0 : 0.0;
+  const double jit = jittered(id) ? cs->p_g / 8.0 : 0.0;
   double vol0 = powern(cs->p_sz, D);
   double h0 = 3.2 / 2. * cs->p_sz;
   double ps[3];
@@ -157,7 +169,7 @@ int pgdg_case_particles(const pgdg_case* cs, int id, uint64_t seed, pgdg_particl
 }
 
 int pgdg_case_cells(const pgdg_case* cs, pgdg_cells* c) {
-  const int D = cs->dim, F = 2, U = D + 2, B = D + 1;
+  const int D = cs->dim, F = cs->nfld, U = D + 2, B = D + 1;
   int64_t n = (int64_t)cs->ncell[0] * cs->ncell[1] * (D == 3 ? cs->ncell[2] : 1);
   if (!c || c->n != n) return PGDG_EINVAL;
   for (int64_t ci = 0; ci < n; ci++) {

@@ -71,10 +71,20 @@ PGDG_CHD Region region_of(int id, const double* x, const double* ps) {
       else r = {1, 1000.0, 1e5, {0, 0, 0}};
       break;
     }
+    case 5:
+      /* three materials (Triple_point_3phase/mpm_ini.cpp:157-245): lower right
+       * phase 1, upper right phase 2, left phase 3 */
+      if (x[0] > 1.0 && x[1] < 1.5) r = {1, 1.0, 0.1, {0, 0, 0}};
+      else if (x[0] > 1.0) r = {2, 0.125, 0.1, {0, 0, 0}};
+      else r = {3, 1.0, 1.0, {0, 0, 0}};
+      break;
     default: break;
   }
   return r;
 }
+
+/* the triple-point layouts jitter their sub-lattice (seeded, +-p_g/8) */
+PGDG_CHD bool jittered(int id) { return id == 1 || id == 5; }
 
 /* the particle at lattice index (i, j, k), number p: position (with the
  * triple point's jitter, draws D p + d of the stream), region and state */

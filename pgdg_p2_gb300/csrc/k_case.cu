@@ -24,7 +24,7 @@ using namespace pgdg_case_math;
 
 struct CaseGen {
   int id, D, na[3];
-  double box_l[3], p_sz, jit, vol0, h0, gam[2], pinf[2], ps[3], c_ini[2];
+  double box_l[3], p_sz, jit, vol0, h0, gam[PGDG_MAX_FLD], pinf[PGDG_MAX_FLD], ps[3], c_ini[PGDG_MAX_FLD];
   uint64_t seed;
 };
 
@@ -100,12 +100,12 @@ int case_build(const CaseK& K, const DevPtrs<R>& P, const pgdg_case& cs, int id,
     G.box_l[d] = cs.box_l[d];
   }
   G.p_sz = cs.p_sz;
-  G.jit = (id == 1) ? cs.p_g / 8.0 : 0.0;
+  G.jit = jittered(id) ? cs.p_g / 8.0 : 0.0;
   double vol0 = 1;
   for (int d = 0; d < D; d++) vol0 *= cs.p_sz;
   G.vol0 = vol0;
   G.h0 = 3.2 / 2. * cs.p_sz;
-  for (int s = 0; s < 2; s++) {
+  for (int s = 0; s < F; s++) {
     G.gam[s] = cs.gamma[s];
     G.pinf[s] = cs.pinf[s];
     G.c_ini[s] = cs.c_ini[s];
@@ -122,11 +122,15 @@ int case_build(const CaseK& K, const DevPtrs<R>& P, const pgdg_case& cs, int id,
 
 template int case_build<2, float>(const CaseK&, const DevPtrs<float>&, const pgdg_case&, int, uint64_t, int64_t,
                                   cudaStream_t);
+#if PGDG_WITH_3D
 template int case_build<3, float>(const CaseK&, const DevPtrs<float>&, const pgdg_case&, int, uint64_t, int64_t,
                                   cudaStream_t);
+#endif
 template int case_build<2, double>(const CaseK&, const DevPtrs<double>&, const pgdg_case&, int, uint64_t, int64_t,
                                    cudaStream_t);
+#if PGDG_WITH_3D
 template int case_build<3, double>(const CaseK&, const DevPtrs<double>&, const pgdg_case&, int, uint64_t, int64_t,
                                    cudaStream_t);
+#endif
 
 }  // namespace pgdg

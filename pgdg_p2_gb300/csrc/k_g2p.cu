@@ -143,14 +143,20 @@ __global__ void __launch_bounds__(128, minblocks_f32<R>(8)) k_g2p(CaseK K, DevPt
     P.c[p] = c;
     HN[p] = hroot<D, R>(vol);
     /* the shifting sum's record: position and volume, the phase in the
-     * volume's sign (two phases), density and sound speed apart (read only
-     * for pairs across the interface) */
-    static_assert(F == 2, "the record's sign carries one of two phases");
+     * volume's sign (two phases) or, with three (2D only), in the unused z
+     * slot; density and sound speed apart (read only for pairs across the
+     * interface) */
+    static_assert(F == 2 || D == 2, "three materials: the record's z slot carries the phase (2D)");
     typename Vec4<R>::T r4;
     r4.x = x[0];
     r4.y = x[1];
-    r4.z = (D == 3) ? x[2] : R(0);
-    r4.w = copysign(vol, ph == 2 ? R(-1) : R(1));
+    if constexpr (F == 2) {
+      r4.z = (D == 3) ? x[2] : R(0);
+      r4.w = copysign(vol, ph == 2 ? R(-1) : R(1));
+    } else {
+      r4.z = R(ph);
+      r4.w = vol;
+    }
     reinterpret_cast<typename Vec4<R>::T*>(P.rec)[p] = r4;
     typename Vec2<R>::T r2;
     r2.x = rho;
@@ -419,15 +425,16 @@ __device__ __forceinline__ void pst_boundary_cell(const CaseK& K, const DevPtrs<
 
 /* a member's contribution from the record G2P wrote: (new x, signed volume),
  * with density and sound speed in the second array */
-template <typename R>
-__device__ __forceinline__ int rec_phase(R w) {
-  return signbit(w) ? 2 : 1;
+template <typename V4>
+__device__ __forceinline__ int rec_phase(const V4& r) {
+  if constexpr (F == 2) return signbit(r.w) ? 2 : 1;
+  else return (int)r.z;
 }
 template <int D, typename R, bool EX>
 __device__ __forceinline__ void pst_rec_add(const DevPtrs<R>& P, int32_t q, const typename Vec4<R>::T& a,
                                             PstPart<D, R, EX>& pp) {
   R xnq[3] = {a.x, a.y, a.z};
-  pp.add(xnq, fabs(a.w), rec_phase(a.w), P.rec2 + 2 * (int64_t)q, nullptr);
+  pp.add(xnq, fabs(a.w), rec_phase(a), P.rec2 + 2 * (int64_t)q, nullptr);
 }
 template <int D, typename R, bool EX>
 __device__ __forceinline__ void pst_rec(const DevPtrs<R>& P, int32_t q, PstPart<D, R, EX>& pp) {
@@ -817,6 +824,17 @@ __device__ __forceinline__ void pst_finish(const CaseK& K, const DevPtrs<R>& P, 
       R ds = (pp.xnp[a] - cen) * nn;
       if (ds < R(0)) nn = -nn;
       R dis = fabs(ds);
+      if constexpr (!EX) {
+        /* a particle exactly on the wall (far likelier with FP32 coordinates):
+         * the reference's 0.02 / dis is infinite there, and the capped
+         * displacement of Update_PST turns it into NaN (inf x 0).  Take the
+         * limit dis -> 0 from the domain side instead: a finite push away from
+         * the wall, which the cap below limits to p_sz / 2 */
+        if (!(dis > R(0))) {
+          dis = R(1e-6) * (R)K.p_sz;
+          nn = R(-sg);
+        }
+      }
       if (dis < R(0.4) * (R)K.p_sz) bp[a] += R(0.02) / dis * (pp.c_p * pp.c_p) * nn;
     }
   }
@@ -1465,7 +1483,7 @@ __device__ __forceinline__ void pst2_rows(const CaseK& K, const DevPtrs<R>& P, c
               if constexpr (D == 3) pp.pst[2] = fmaf(drz.y, f.y, pp.pst[2]);
             }
             /* across the interface: the sharpening term (rare) */
-            const bool xa = ka && rec_phase(ra.w) != pp.ph, xb = kb && rec_phase(rb.w) != pp.ph;
+            const bool xa = ka && rec_phase(ra) != pp.ph, xb = kb && rec_phase(rb) != pp.ph;
             if (xa || xb) {
               for (int k = 0; k < 2; k++) {
                 if (!(k == 0 ? xa : xb)) continue;
@@ -1483,11 +1501,11 @@ __device__ __forceinline__ void pst2_rows(const CaseK& K, const DevPtrs<R>& P, c
           } else {
             if (ma) {
               R xnq[3] = {ra.x, ra.y, ra.z};
-              pp.add(xnq, fabs(ra.w), rec_phase(ra.w), P.rec2 + 2 * (int64_t)slot_of<R>(va.w), nullptr);
+              pp.add(xnq, fabs(ra.w), rec_phase(ra), P.rec2 + 2 * (int64_t)slot_of<R>(va.w), nullptr);
             }
             if (mb) {
               R xnq[3] = {rb.x, rb.y, rb.z};
-              pp.add(xnq, fabs(rb.w), rec_phase(rb.w), P.rec2 + 2 * (int64_t)slot_of<R>(vb.w), nullptr);
+              pp.add(xnq, fabs(rb.w), rec_phase(rb), P.rec2 + 2 * (int64_t)slot_of<R>(vb.w), nullptr);
             }
           }
         }
@@ -1795,12 +1813,18 @@ void Launch<D, R, EX>::pst(const CaseK& K, const DevPtrs<R>& P, int xs, int hs, 
   template int Launch<D, R, EX>::pst_variants();
 #ifdef PGDG_EXACT_TU
 PGDG_INST(2, double, true)
+#if PGDG_WITH_3D
 PGDG_INST(3, double, true)
+#endif
 #else
 PGDG_INST(2, double, false)
+#if PGDG_WITH_3D
 PGDG_INST(3, double, false)
+#endif
 PGDG_INST(2, float, false)
+#if PGDG_WITH_3D
 PGDG_INST(3, float, false)
+#endif
 #endif
 
 }  // namespace pgdg

@@ -1249,12 +1249,14 @@ __device__ __forceinline__ void dd_merge(DD& a, const DD& b) {
   a.lo += b.lo;
 }
 constexpr int TOT_BLOCKS = 304, TOT_THREADS = 256;
+/* totals: particle mass per phase, particle energy, cell mass per phase, cell energy */
+constexpr int NTOT = 2 * F + 2;
 constexpr size_t PROBE_DOUBLES = 6 * (size_t)TOT_BLOCKS; /* the bubble probe's block partials */
 /* the blocks' partial sums in block order, rounded once */
 __global__ void k_totals_final(const DD* part, double* out) {
-  if (threadIdx.x < 6) {
+  if (threadIdx.x < NTOT) {
     DD t = part[threadIdx.x];
-    for (int b = 1; b < TOT_BLOCKS; b++) dd_merge(t, part[b * 6 + threadIdx.x]);
+    for (int b = 1; b < TOT_BLOCKS; b++) dd_merge(t, part[b * NTOT + threadIdx.x]);
     out[threadIdx.x] = t.hi + t.lo;
   }
 }
@@ -1280,8 +1282,8 @@ __global__ void k_probe_final(const double* part, double* out) {
 
 template <int D, typename R, bool EX>
 __global__ void __launch_bounds__(TOT_THREADS) k_totals(CaseK K, DevPtrs<R> P, DD* part) {
-  DD acc[6];
-  for (int k = 0; k < 6; k++) acc[k] = DD{0.0, 0.0};
+  DD acc[NTOT];
+  for (int k = 0; k < NTOT; k++) acc[k] = DD{0.0, 0.0};
   const int64_t n = (int64_t)P.cnt->n_slots;
   GRID_STRIDE(p, n) {
     int ph = P.phase[p];
@@ -1289,7 +1291,7 @@ __global__ void __launch_bounds__(TOT_THREADS) k_totals(CaseK K, DevPtrs<R> P, D
     dd_add(acc[ph - 1], (double)P.rho[p] * (double)P.vol[p]);
     double e = (double)P.E[p];
     if (K.eshift[ph - 1] != 0.0) e += K.eshift[ph - 1];
-    dd_add(acc[2], e * (double)P.vol[p]);
+    dd_add(acc[F], e * (double)P.vol[p]);
   }
   const int64_t nc = K.ncell;
   double voli = K.ps[0] * K.ps[1] * (D == 3 ? K.ps[2] : 1.0);
@@ -1298,15 +1300,15 @@ __global__ void __launch_bounds__(TOT_THREADS) k_totals(CaseK K, DevPtrs<R> P, D
     for (int s = 0; s < F; s++) {
       if (P.cph[s * nc + ci] != 1) continue;
       double a = (double)P.calph[s * nc + ci];
-      dd_add(acc[3 + s], voli * a * (double)P.crho[s * nc + ci]);
+      dd_add(acc[F + 1 + s], voli * a * (double)P.crho[s * nc + ci]);
       double e = (double)P.cE[s * nc + ci];
       if (K.eshift[s] != 0.0) e += K.eshift[s];
-      dd_add(acc[5], voli * a * e);
+      dd_add(acc[2 * F + 1], voli * a * e);
     }
   }
-  __shared__ DD s_w[TOT_THREADS / 32][6];
+  __shared__ DD s_w[TOT_THREADS / 32][NTOT];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int k = 0; k < 6; k++) {
+  for (int k = 0; k < NTOT; k++) {
     for (int o = 16; o > 0; o >>= 1) {
       DD b{__shfl_down_sync(0xffffffffu, acc[k].hi, o), __shfl_down_sync(0xffffffffu, acc[k].lo, o)};
       if (lane + o < 32) dd_merge(acc[k], b);
@@ -1314,23 +1316,23 @@ __global__ void __launch_bounds__(TOT_THREADS) k_totals(CaseK K, DevPtrs<R> P, D
     if (lane == 0) s_w[w][k] = acc[k];
   }
   __syncthreads();
-  if (threadIdx.x < 6) {
+  if (threadIdx.x < NTOT) {
     DD t = s_w[0][threadIdx.x];
     for (int v = 1; v < TOT_THREADS / 32; v++) dd_merge(t, s_w[v][threadIdx.x]);
-    part[blockIdx.x * 6 + threadIdx.x] = t;
+    part[blockIdx.x * NTOT + threadIdx.x] = t;
   }
 }
 
 template <int D, typename R, bool EX>
-void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out6, cudaStream_t st) {
-  /* d_out6 holds 6 results followed by the blocks' partials (totals_scratch) */
-  DD* part = reinterpret_cast<DD*>(d_out6 + 6);
+void Launch<D, R, EX>::totals(const CaseK& K, const DevPtrs<R>& P, double* d_out, cudaStream_t st) {
+  /* d_out holds the 2F + 2 results followed by the blocks' partials (totals_scratch) */
+  DD* part = reinterpret_cast<DD*>(d_out + NTOT + (NTOT & 1));
   k_totals<D, R, EX><<<TOT_BLOCKS, TOT_THREADS, 0, st>>>(K, P, part);
-  k_totals_final<<<1, 32, 0, st>>>(part, d_out6);
+  k_totals_final<<<1, 32, 0, st>>>(part, d_out);
 }
 template <int D, typename R, bool EX>
 size_t Launch<D, R, EX>::totals_scratch() {
-  return 6 + 2 * 6 * (size_t)TOT_BLOCKS + PROBE_DOUBLES;
+  return NTOT + (NTOT & 1) + 2 * NTOT * (size_t)TOT_BLOCKS + PROBE_DOUBLES;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1428,12 +1430,18 @@ void Launch<D, R, EX>::probe(const CaseK& K, const DevPtrs<R>& P, double* d_scra
   template void Launch<D, R, EX>::probe(const CaseK&, const DevPtrs<R>&, double*, double*, cudaStream_t);
 #ifdef PGDG_EXACT_TU
 PGDG_INST(2, double, true)
+#if PGDG_WITH_3D
 PGDG_INST(3, double, true)
+#endif
 #else
 PGDG_INST(2, double, false)
+#if PGDG_WITH_3D
 PGDG_INST(3, double, false)
+#endif
 PGDG_INST(2, float, false)
+#if PGDG_WITH_3D
 PGDG_INST(3, float, false)
+#endif
 #endif
 
 }  // namespace pgdg

@@ -154,12 +154,18 @@ void output_pack_cells(const CaseK& K, const DevPtrs<R>& P, double* dc, cudaStre
   template void output_pack_cells<D, R, EX>(const CaseK&, const DevPtrs<R>&, double*, cudaStream_t);
 #ifdef PGDG_EXACT_TU
 PGDG_OUT_INST(2, double, true)
+#if PGDG_WITH_3D
 PGDG_OUT_INST(3, double, true)
+#endif
 #else
 PGDG_OUT_INST(2, double, false)
+#if PGDG_WITH_3D
 PGDG_OUT_INST(3, double, false)
+#endif
 PGDG_OUT_INST(2, float, false)
+#if PGDG_WITH_3D
 PGDG_OUT_INST(3, float, false)
+#endif
 #endif
 
 }  // namespace pgdg

@@ -940,10 +940,16 @@ void Launch<D, R, EX>::reset_lists(const CaseK& K, const DevPtrs<R>& P, cudaStre
   template void Launch<D, R, EX>::store_lists(const CaseK&, const DevPtrs<R>&, int, int, int, cudaStream_t); \
   template void Launch<D, R, EX>::reset_lists(const CaseK&, const DevPtrs<R>&, cudaStream_t);
 PGDG_INST(2, double, false)
+#if PGDG_WITH_3D
 PGDG_INST(3, double, false)
+#endif
 PGDG_INST(2, float, false)
+#if PGDG_WITH_3D
 PGDG_INST(3, float, false)
+#endif
 PGDG_INST(2, double, true)
+#if PGDG_WITH_3D
 PGDG_INST(3, double, true)
+#endif
 
 }  // namespace pgdg

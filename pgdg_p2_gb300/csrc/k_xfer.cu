@@ -24,15 +24,26 @@ inline int xgrid(int64_t n) {
   return g < 1 ? 1 : (int)g;
 }
 
+/* the per-group shifts of a transfer (a particle's energy by its phase, one
+ * group per material), passed by value */
+struct GroupShift {
+  double g[F];
+  __device__ __forceinline__ double of(int grp1) const {
+    const int k = grp1 - 1;
+    return (k >= 0 && k < F) ? g[k] : 0.0;
+  }
+};
+inline GroupShift group_shift(const double* gsh) {
+  GroupShift s{};
+  for (int k = 0; k < F; k++) s.g[k] = gsh ? gsh[k] : 0.0;
+  return s;
+}
+
 template <typename R>
 __global__ void k_h2d(const double* __restrict__ h, int hstride, int64_t i0, int64_t m, XferMap km,
-                      R* __restrict__ d, int64_t dstride, const int8_t* __restrict__ grp, double g0, double g1) {
+                      R* __restrict__ d, int64_t dstride, const int8_t* __restrict__ grp, GroupShift gsh) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-    double gs = 0.0;
-    if (grp) {
-      const int g = grp[i0 + i] - 1;
-      gs = g == 0 ? g0 : (g == 1 ? g1 : 0.0);
-    }
+    const double gs = grp ? gsh.of(grp[i0 + i]) : 0.0;
     for (int k = 0; k < km.n; k++) {
       double x = h[i * hstride + km.hk[k]];
       if (km.sh[k] != 0.0) x -= km.sh[k];
@@ -45,14 +56,10 @@ __global__ void k_h2d(const double* __restrict__ h, int hstride, int64_t i0, int
 template <typename R>
 __global__ void k_d2h(const R* __restrict__ d, int64_t dstride, const int64_t* __restrict__ idx, int64_t i0,
                       int64_t m, XferMap km, double* __restrict__ h, int hstride, const int8_t* __restrict__ grp,
-                      double g0, double g1) {
+                      GroupShift gsh) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t src = idx ? idx[i0 + i] : i0 + i;
-    double gs = 0.0;
-    if (grp) {
-      const int g = grp[src] - 1;
-      gs = g == 0 ? g0 : (g == 1 ? g1 : 0.0);
-    }
+    const double gs = grp ? gsh.of(grp[src]) : 0.0;
     for (int k = 0; k < km.n; k++) {
       double x = (double)d[k * dstride + src];
       if (km.sh[k] != 0.0) x += km.sh[k];
@@ -121,14 +128,13 @@ template <typename R>
 cudaError_t xfer_h2d(const double* host, int hstride, int64_t n, const XferMap& km, R* dev, int64_t dstride,
                      const int8_t* grp, const double* gsh, XferStage& sg, cudaStream_t st) {
   const int64_t per = (int64_t)(sg.bytes / (sizeof(double) * (size_t)hstride));
-  const double g0 = gsh ? gsh[0] : 0.0, g1 = gsh ? gsh[1] : 0.0;
+  const GroupShift gs = group_shift(gsh);
   for (int64_t i0 = 0; i0 < n; i0 += per) {
     const int64_t m = n - i0 < per ? n - i0 : per;
     cudaError_t e = cudaMemcpyAsync(sg.buf, host + i0 * hstride, sizeof(double) * (size_t)(m * hstride),
                                     cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
-    k_h2d<R><<<xgrid(m), XB, 0, st>>>(static_cast<const double*>(sg.buf), hstride, i0, m, km, dev, dstride, grp, g0,
-                                      g1);
+    k_h2d<R><<<xgrid(m), XB, 0, st>>>(static_cast<const double*>(sg.buf), hstride, i0, m, km, dev, dstride, grp, gs);
   }
   return cudaGetLastError();
 }
@@ -137,12 +143,12 @@ template <typename R>
 cudaError_t xfer_d2h(const R* dev, int64_t dstride, const int64_t* idx, int64_t n, const XferMap& km, double* host,
                      int hstride, const int8_t* grp, const double* gsh, XferStage& sg, cudaStream_t st) {
   const int64_t per = (int64_t)(sg.bytes / (sizeof(double) * (size_t)hstride));
-  const double g0 = gsh ? gsh[0] : 0.0, g1 = gsh ? gsh[1] : 0.0;
+  const GroupShift gs = group_shift(gsh);
   for (int64_t i0 = 0; i0 < n; i0 += per) {
     const int64_t m = n - i0 < per ? n - i0 : per;
     cudaError_t e = cudaMemsetAsync(sg.buf, 0, sizeof(double) * (size_t)(m * hstride), st);
     if (e != cudaSuccess) return e;
-    k_d2h<R><<<xgrid(m), XB, 0, st>>>(dev, dstride, idx, i0, m, km, static_cast<double*>(sg.buf), hstride, grp, g0, g1);
+    k_d2h<R><<<xgrid(m), XB, 0, st>>>(dev, dstride, idx, i0, m, km, static_cast<double*>(sg.buf), hstride, grp, gs);
     e = cudaMemcpyAsync(host + i0 * hstride, sg.buf, sizeof(double) * (size_t)(m * hstride), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) return e;
     e = cudaStreamSynchronize(st);

@@ -20,9 +20,22 @@
 #include "../../include/pgdg_types.h"
 #include "pgdg_math.cuh"
 
+/* FldNum (glbparam.h:41): the number of materials is a compile-time constant,
+ * as in the reference, which builds one binary per material count.  The
+ * default build holds two materials (every 2D and 3D workload); a build with
+ * -DPGDG_NFLD=3 holds the 2D three-material instance (Triple_point_3phase). */
+#ifndef PGDG_NFLD
+#define PGDG_NFLD 2
+#endif
+#if PGDG_NFLD == 2
+#define PGDG_WITH_3D 1
+#else
+#define PGDG_WITH_3D 0
+#endif
+
 namespace pgdg {
 
-constexpr int F = 2;
+constexpr int F = PGDG_NFLD;
 /* list-order keys (Cell_list order): base entries are ordered by slot,
  * appended entries (Add_particle during split/merge) by an append counter */
 constexpr uint32_t KEY_APPEND = 0x80000000u;
@@ -221,8 +234,10 @@ struct Launch {
   static void iface_gather(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t);
   static void grid_acc_queued(const CaseK&, const DevPtrs<R>&, IfaceQ, cudaStream_t);
   static void update_grid(const CaseK&, const DevPtrs<R>&, int md, cudaStream_t);
-  static void totals(const CaseK&, const DevPtrs<R>&, double* d_out6, cudaStream_t);
-  static size_t totals_scratch(); /* doubles d_out6 must hold */
+  /* 2F + 2 totals into d_out: particle mass per phase, particle energy, cell
+   * mass per phase, cell energy */
+  static void totals(const CaseK&, const DevPtrs<R>&, double* d_out, cudaStream_t);
+  static size_t totals_scratch(); /* doubles d_out must hold */
   /* bubble probe (downstream end, jet, upstream end, phase-2 mass, fluid
    * count) into d_out5, with the totals scratch for its partials */
   static void probe(const CaseK&, const DevPtrs<R>&, double* d_scratch, double* d_out5, cudaStream_t);

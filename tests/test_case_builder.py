@@ -66,7 +66,7 @@ def test_undex_stiffened_gas():
 
 @pytest.mark.parametrize("cid,grid,seed", [(1, None, 0), (1, (56, 24), 77), (2, (32, 8, 8), 0), (3, (48, 12, 12), 0),
                                            (3, (96, 24, 24), 0), (4, (64, 64), 0), (2, None, 0), (3, None, 0),
-                                           (4, None, 0)])
+                                           (4, None, 0), (5, None, 0), (5, (56, 24), 9)])
 def test_oracle_case_builder_bitwise(cid, grid, seed):
     """The oracle's own case construction (used by the CPU arms of the bench,
     which load no GPU library) equals the library's bit for bit: the case
@@ -84,3 +84,18 @@ def test_oracle_case_builder_bitwise(cid, grid, seed):
     for k in ("rho", "rhov", "E", "c", "ac", "alph", "coef", "v", "P", "ph_state", "ph_state_b", "used", "lim_u",
               "g_v", "dcoef"):
         assert getattr(cg, k).tobytes() == getattr(co, k).tobytes(), k
+
+
+def test_three_material_regions():
+    """Triple_point_3phase (mpm_ini.cpp:80-97, 157-245): lower right phase 1,
+    upper right phase 2, left phase 3 (stiffened, p_inf 0.1), on C1's box."""
+    cs, p, c = M.make_case(5)
+    assert cs.nfld == 3 and cs.dim == 2 and tuple(cs.ncell[:2]) == (112, 48)
+    assert list(cs.gamma) == [1.4, 1.5, 1.6] and list(cs.pinf) == [0, 0, 0.1]
+    x, y = p.coord[:, 0], p.coord[:, 1]
+    assert np.all(p.phase[(x > 1) & (y < 1.5)] == 1)
+    assert np.all(p.phase[(x > 1) & (y >= 1.5)] == 2)
+    assert np.all(p.phase[x <= 1] == 3)
+    left = p.phase == 3
+    assert np.allclose(p.P[left], 1.0) and np.allclose(p.E[left], (1.0 + 1.6 * 0.1) / 0.6)
+    assert c.rho.shape == (cs.ncells, 3)

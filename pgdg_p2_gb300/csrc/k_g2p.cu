@@ -1542,8 +1542,7 @@ __global__ void __launch_bounds__(512, SREC ? 1 : 2) k_pst2(CaseK K, DevPtrs<R> 
   const int nsc = sn[0] * sn[1] * sn[2];
   const int nrow = (D == 3) ? sn[0] * sn[1] : sn[0];
   constexpr int RA = D - 1;
-  /* shared layout: off[nrow+1] | rsrc[nrow] | rlo[2 nrow] | rhi[2 nrow] | boundary cells[nsc] | ent[cap] |
-   * rec[cap] | tag[cap] */
+  /* shared layout: off[nrow+1] | rsrc[nrow] | rlo[2 nrow] | rhi[2 nrow] | bnd[nsc] | ent[cap] | rec[cap] | tag[cap] */
   size_t o = 0;
   auto take = [&](size_t bytes, size_t al) {
     o = (o + al - 1) / al * al;
@@ -1560,24 +1559,10 @@ __global__ void __launch_bounds__(512, SREC ? 1 : 2) k_pst2(CaseK K, DevPtrs<R> 
   V4* s_rec = SREC ? reinterpret_cast<V4*>(take(sizeof(V4) * cap, 32)) : nullptr;
   unsigned char* s_tag = take(cap, 16);
   __shared__ int s_red[SCAN_RED];
-  /* the staged cells holding boundary particles, in ascending order (the order
-   * in which the direct variants scan a particle's window) */
-  __shared__ int s_nbc;
-  if (threadIdx.x < 32) {
-    int cnt = 0;
-    for (int l0 = 0; l0 < nsc; l0 += 32) {
-      const int l = l0 + threadIdx.x;
-      bool has = false;
-      if (l < nsc) {
-        const int t = l / (sn[1] * sn[2]), s = (l / sn[2]) % sn[1], m = l % sn[2];
-        const int64_t c = ((int64_t)(slo[0] + t) * K.N[1] + (slo[1] + s)) * K.N[2] + (slo[2] + m);
-        has = P.boff[c + 1] > P.boff[c];
-      }
-      const unsigned bal = __ballot_sync(0xffffffffu, has);
-      if (has) s_bnd[cnt + __popc(bal & ((1u << threadIdx.x) - 1u))] = l;
-      cnt += __popc(bal);
-    }
-    if (threadIdx.x == 0) s_nbc = cnt;
+  for (int l = threadIdx.x; l < nsc; l += blockDim.x) {
+    const int t = l / (sn[1] * sn[2]), s = (l / sn[2]) % sn[1], m = l % sn[2];
+    const int64_t c = ((int64_t)(slo[0] + t) * K.N[1] + (slo[1] + s)) * K.N[2] + (slo[2] + m);
+    s_bnd[l] = P.boff[c + 1] > P.boff[c] ? 1 : 0;
   }
   const int NR = K.N[RA];
   for (int row = threadIdx.x; row < nrow; row += blockDim.x) {
@@ -1692,13 +1677,14 @@ __global__ void __launch_bounds__(512, SREC ? 1 : 2) k_pst2(CaseK K, DevPtrs<R> 
     bool edge = false;
     for (int d = 0; d < D; d++) edge = edge || lo[d] == 0 || hi[d] == K.N[d] - 1;
     if (edge)
-      for (int k = 0; k < s_nbc; k++) {
-        const int l = s_bnd[k];
-        const int t = slo[0] + l / (sn[1] * sn[2]), s = slo[1] + (l / sn[2]) % sn[1], m = slo[2] + l % sn[2];
-        if (t < lo[0] || t > hi[0] || s < lo[1] || s > hi[1] || m < lo[2] || m > hi[2]) continue;
-        const int64_t cc = ((int64_t)t * K.N[1] + s) * K.N[2] + m;
-        pst_boundary_cell<D, R, false>(K, P, cc, pp);
-      }
+      for (int t = lo[0]; t <= hi[0]; t++)
+        for (int s = lo[1]; s <= hi[1]; s++)
+          for (int m = lo[2]; m <= hi[2]; m++) {
+            const int l = ((t - slo[0]) * sn[1] + (s - slo[1])) * sn[2] + (m - slo[2]);
+            if (!s_bnd[l]) continue;
+            const int64_t cc = ((int64_t)t * K.N[1] + s) * K.N[2] + m;
+            pst_boundary_cell<D, R, false>(K, P, cc, pp);
+          }
     pst_finish<D, R, false>(K, P, p, dt, pp);
   }
 }
